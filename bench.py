@@ -1,0 +1,345 @@
+"""Benchmark of the IMEXLBM time step on GB300.
+
+Workload: the shipped deck size - 256^3 fully periodic Taylor-Green vortex,
+rho0 = 1, Re = 1600, u0 = 0.05, float64 distributions (two arrays of
+27 x 256^3 doubles, 3.62 GB each), reporting every 100 steps.  One "step" is
+one reference time step (collision + pull streaming) of the whole lattice.
+
+  value  MLUPS of K device-resident steps, CUDA events on the lattice's
+         stream (the reference's MLUPS, src/main.cpp:71-80, also excludes
+         the diagnostics); the arrays are larger than L2, so no flush.
+  e2e    the same metric through the public C ABI with host buffers: upload
+         f0 from pinned host memory, K steps with the Conserved diagnostics
+         read back every 100 steps, download f at the end - all timed.
+  roofline  the fused step kernel: algorithmic 432 B/cell (27 float64 read
+         + 27 written) x cells / average launch time, against the measured
+         HBM copy bandwidth.
+  cpu_baseline  the CPU oracle (a C restatement of the reference's step,
+         OpenMP on all host cores) on a bounded sample of the workload.
+
+--impl reference times that CPU oracle alone on the same metric (the
+reference itself cannot be built here: it needs Kokkos and MPI).
+
+Multi-GPU: the path does not shard on a one-GPU machine; under torchrun each
+rank advances its own independent lattice (replicas, weak scaling) and
+value = all ranks' cell updates / the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+BYTES_PER_CELL_F64 = 432  # 27 float64 read + 27 written per cell update
+FLOP_PER_CELL = 594       # the reference's own count (src/profile.cpp:38)
+DECK = "1.0 0.1 1600\n0.05 1000 100\n256 256 256\n"
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse_args(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--engine", choices=["auto", "native", "fixed"], default="auto")
+    ap.add_argument("--size", type=int, default=256, help="cubic lattice edge (default: the shipped deck's 256)")
+    ap.add_argument("--report-every", type=int, default=100)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args(argv)
+
+
+# ----------------------------------------------------------------- helpers --
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as fp:
+            d = json.load(fp)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def load_traffic(kernel: str):
+    """Per-cell DRAM bytes of `kernel` from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "dram_traffic.json")
+    try:
+        with open(p) as fp:
+            d = json.load(fp)
+        return d[kernel]
+    except Exception:
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason sampling during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.rows = []
+        if self.proc is None:
+            return
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=10)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        for ln in out.splitlines():
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) == 8:
+                self.rows.append(parts)
+
+    def summary(self):
+        if not getattr(self, "rows", None):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[4 + i].lower() == "active"})
+        # median under load: samples at or above half the max clock
+        top = max(sm) if sm else 0.0
+        load = [s for s in sm if s >= 0.5 * top] or sm
+        return {"sm_mhz": statistics.median(load) if load else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(sm)}
+
+
+def dist_env():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+# -------------------------------------------------------------- CPU timing --
+def time_cpu_oracle(n: int, tau: float, steps: int, warmup: int, budget_s: float):
+    """Time the oracle on an n x n x nz slab with nz chosen so that
+    steps + warmup slab steps fit in about budget_s seconds."""
+    import numpy as np
+
+    from oracle import oracle as o
+    o.build()
+    threads = o.max_threads()
+    o.set_threads(threads)
+    # calibrate on a thin slab
+    nz_cal = max(1, min(n, 8))
+    f = o.init(n, n, nz_cal, 1.0, 0.05)
+    ft = np.empty_like(f)
+    o.step_pingpong(f, ft, tau)
+    t = time.perf_counter()
+    o.step_pingpong(ft, f, tau)
+    per_cell = (time.perf_counter() - t) / (n * n * nz_cal)
+    total = max(1, steps + warmup)
+    nz = int(max(1, min(n, budget_s / total / max(per_cell * n * n, 1e-12))))
+    f = o.init(n, n, nz, 1.0, 0.05)
+    ft = np.empty_like(f)
+    for _ in range(warmup):
+        o.step_pingpong(f, ft, tau)
+        f, ft = ft, f
+    t = time.perf_counter()
+    for _ in range(steps):
+        o.step_pingpong(f, ft, tau)
+        f, ft = ft, f
+    dt = time.perf_counter() - t
+    cells = n * n * nz
+    return {"value": cells * steps / dt / 1e6, "unit": "MLUPS", "cores": threads, "kind": "port",
+            "sample": f"{n}x{n}x{nz} slab (of {n}^3), {steps} steps after {warmup} warm-up, "
+                      f"float64 collide+stream, OpenMP {threads} threads",
+            "seconds": dt}
+
+
+def run_reference(a):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    d = parse_deck_text(a.size)
+    steps = max(1, a.steps)
+    cb = time_cpu_oracle(a.size, d["tau"], steps, max(0, a.warmup), budget_s=120.0)
+    line = {"impl": "reference", "metric": "MLUPS", "value": round(cb["value"], 3), "unit": "MLUPS",
+            "n_gpus": a.gpus, "steps": steps, "warmup": a.warmup,
+            "ms_per_step": round(cb["seconds"] / steps * 1e3, 4), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic: Taylor-Green initial field",
+            "config": workload_config(a, "oracle"),
+            "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "e2e": {"value": round(cb["value"], 3), "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "reference sources need Kokkos + MPI (absent): this is the CPU oracle, a C restatement of "
+                    "src/lbm.cpp:78-207 run with OpenMP on all host cores"}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def parse_deck_text(n):
+    from oracle import oracle as o
+    o.build()
+    d = o.parse_deck(f"1.0 0.1 1600\n0.05 1000 100\n{n} {n} {n}\n")
+    return {"tau": d.tau, "rho0": d.rho0, "u0": d.u0}
+
+
+def workload_config(a, engine):
+    return {"workload": f"taylor-green {a.size}^3 periodic D3Q27, Re=1600, u0=0.05, float64 distributions",
+            "grid": [a.size] * 3, "precision": "f64", "engine": engine, "report_every": a.report_every,
+            "l2": "inputs larger than L2 (2 arrays x %.2f GB), no flush" % (27 * a.size ** 3 * 8 / 1e9),
+            "parallelism": "replicas (one independent lattice per GPU)"}
+
+
+# ------------------------------------------------------------------ GPU arm --
+def run_ours(a):
+    import numpy as np
+    import torch
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    import imexlbm_gb300 as m
+    m.load()
+    d = parse_deck_text(a.size)
+    n = a.size
+    cells = n ** 3
+    engine = {"auto": m.IMEX_ENGINE_AUTO, "native": m.IMEX_ENGINE_NATIVE, "fixed": m.IMEX_ENGINE_FIXED}[a.engine]
+    stream = torch.cuda.Stream()
+    lat = m.LBM(n, n, n, d["tau"], d["rho0"], d["u0"], engine=engine)
+    lat.set_stream(stream.cuda_stream)
+    lat.Initialize()
+    eng_name = "fixed" if (engine == m.IMEX_ENGINE_FIXED) else "native" if engine == m.IMEX_ENGINE_NATIVE else "auto"
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    # warm-up (includes the first-step collide-only kernel)
+    lat.step(max(3, a.warmup))
+    lat.fence()
+    torch.cuda.synchronize()
+    barrier()
+    lat.fallback_cells(reset=True)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches0 = lat.kernel_launches()
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        barrier()
+        ev0.record(stream)
+        lat.step(a.steps)
+        ev1.record(stream)
+        ev1.synchronize()
+    torch.cuda.synchronize()
+    gpu_launches = lat.kernel_launches() - launches0
+    ms = ev0.elapsed_time(ev1)
+    fallback = lat.fallback_cells(reset=True)
+    t_max = ms
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_max = float(t.item())
+    value = cells * a.steps * world / (t_max * 1e-3) / 1e6
+    cons = lat.Conserved()
+
+    # roofline of the fused step kernel: every timed launch is that kernel
+    hbm, peak_kind = load_peaks()
+    launch_ms = ms / max(1, gpu_launches)
+    achieved = BYTES_PER_CELL_F64 * cells / (launch_ms * 1e-3) / 1e9
+    kname = "step_fx" if eng_name != "native" else "step_f64"
+    tr = load_traffic(kname)
+    roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
+            "frac": round(achieved / hbm, 4), "peak_kind": peak_kind,
+            "traffic": round(tr * cells, 0) if tr is not None else None,
+            "kernel": kname, "algorithmic_bytes_per_launch": BYTES_PER_CELL_F64 * cells}
+
+    # end-to-end through the public API with host buffers
+    e2e = None
+    if not a.no_e2e:
+        nval = 27 * cells
+        host = torch.empty(nval, dtype=torch.float64, pin_memory=True)
+        lat2 = m.LBM(n, n, n, d["tau"], d["rho0"], d["u0"], engine=engine)
+        lat2.set_stream(stream.cuda_stream)
+        lat2.Initialize()
+        import ctypes
+        L = m.load()
+        dp = ctypes.cast(host.data_ptr(), ctypes.POINTER(ctypes.c_double))
+        L.imex_get_f(lat2.handle, dp, nval)     # f0 into pinned host memory (untimed)
+        lat2.step(3)                             # warm the path
+        lat2.fence()
+        barrier()
+        t0 = time.perf_counter()
+        m._lib.check(L.imex_set_f(lat2.handle, dp, nval), lat2.handle)
+        reports = 0
+        done = 0
+        while done < a.steps:
+            k = min(a.report_every, a.steps - done)
+            lat2.step(k)
+            done += k
+            if done % a.report_every == 0:
+                lat2.Conserved()
+                reports += 1
+        m._lib.check(L.imex_get_f(lat2.handle, dp, nval), lat2.handle)
+        dt = time.perf_counter() - t0
+        if world > 1:
+            import torch.distributed as dist
+            t = torch.tensor([dt], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            dt = float(t.item())
+        lat2.close()
+        e2e = {"value": round(cells * a.steps * world / dt / 1e6, 2), "unit": "MLUPS",
+               "h2d_bytes_per_step": round(nval * 8 / a.steps, 1),
+               "d2h_bytes_per_step": round((nval * 8 + 40 * reports) / a.steps, 1),
+               "what": f"imex_set_f from pinned host, {a.steps} steps with imex_conserved every "
+                       f"{a.report_every}, imex_get_f to pinned host"}
+        del host
+
+    cpu = None
+    if rank == 0 and world == 1 and not a.no_cpu_baseline:
+        cb = time_cpu_oracle(n, d["tau"], steps=2, warmup=1, budget_s=20.0)
+        cpu = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+
+    lat.close()
+    if rank == 0:
+        line = {"metric": "MLUPS", "value": round(value, 2), "unit": "MLUPS", "n_gpus": world, "steps": a.steps,
+                "warmup": max(3, a.warmup), "ms_per_step": round(t_max / a.steps, 4), "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None,
+                "dtype": "s64 fixed-point arithmetic, f64 storage" if eng_name != "native" else "f64",
+                "data": "synthetic: Taylor-Green initial field (deterministic, no seed)",
+                "config": workload_config(a, eng_name), "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
+                "gpu_launches": gpu_launches, "clocks": clk.summary(),
+                "fallback_cells": fallback, "mass": cons[0], "ke": cons[4],
+                "roofline_glups_at_peak": round(hbm * 1e9 / BYTES_PER_CELL_F64 / 1e9, 3)}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def main(argv=None):
+    a = parse_args(argv)
+    if a.impl == "reference":
+        return run_reference(a)
+    return run_ours(a)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

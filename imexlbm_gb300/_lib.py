@@ -1,0 +1,107 @@
+"""ctypes binding of libimexlbm.so (the C ABI in include/imexlbm.h).
+
+The library is built in-tree by ``imexlbm_gb300.build``.  There is no
+fallback: if the shared library is missing, loading raises ``ImportError``
+with the build command, and every compute call goes to the CUDA kernels.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+from .build import LIB
+
+IMEX_OK = 0
+IMEX_ERR_ARG = 1
+IMEX_ERR_CUDA = 2
+IMEX_ERR_MEMORY = 3
+IMEX_ERR_DECK = 4
+IMEX_ERR_NONFINITE = 5
+IMEX_ERR_STATE = 6
+
+IMEX_F64 = 0
+IMEX_F32 = 1
+IMEX_F16DEV = 2
+
+IMEX_ENGINE_AUTO = 0
+IMEX_ENGINE_NATIVE = 1
+IMEX_ENGINE_FIXED = 2
+
+# Every symbol include/imexlbm.h declares, with (restype, argtypes).
+_dp = ctypes.POINTER(ctypes.c_double)
+_h = ctypes.c_void_p
+
+
+class Deck(ctypes.Structure):
+    """struct imex_deck (include/imexlbm.h)."""
+
+    _fields_ = [
+        ("rho0", ctypes.c_double), ("R", ctypes.c_double), ("u0", ctypes.c_double),
+        ("Re", ctypes.c_int), ("Time", ctypes.c_int), ("inter", ctypes.c_int),
+        ("sx", ctypes.c_int), ("sy", ctypes.c_int), ("sz", ctypes.c_int),
+        ("cs2", ctypes.c_double), ("cs", ctypes.c_double), ("Ma", ctypes.c_double),
+        ("miu", ctypes.c_double), ("tau", ctypes.c_double),
+    ]
+
+
+SIGNATURES = {
+    "imex_deck_parse": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(Deck)]),
+    "imex_deck_read": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(Deck)]),
+    "imex_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                   ctypes.c_double, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]),
+    "imex_destroy": (None, [_h]),
+    "imex_initialize": (ctypes.c_int, [_h]),
+    "imex_collision": (ctypes.c_int, [_h]),
+    "imex_streaming": (ctypes.c_int, [_h]),
+    "imex_step": (ctypes.c_int, [_h, ctypes.c_int]),
+    "imex_conserved": (ctypes.c_int, [_h, _dp]),
+    "imex_macroscopic": (ctypes.c_int, [_h, _dp, _dp, _dp, _dp]),
+    "imex_get_f": (ctypes.c_int, [_h, _dp, ctypes.c_size_t]),
+    "imex_set_f": (ctypes.c_int, [_h, _dp, ctypes.c_size_t]),
+    "imex_get_f_device": (ctypes.c_int, [_h, ctypes.c_void_p, ctypes.c_size_t]),
+    "imex_set_f_device": (ctypes.c_int, [_h, ctypes.c_void_p, ctypes.c_size_t]),
+    "imex_set_engine": (ctypes.c_int, [_h, ctypes.c_int]),
+    "imex_set_stream": (ctypes.c_int, [_h, ctypes.c_void_p]),
+    "imex_synchronize": (ctypes.c_int, [_h]),
+    "imex_steps_done": (ctypes.c_int64, [_h]),
+    "imex_kernel_launches": (ctypes.c_int64, [_h]),
+    "imex_fallback_cells": (ctypes.c_int, [_h, ctypes.POINTER(ctypes.c_int64), ctypes.c_int]),
+    "imex_device_bytes": (ctypes.c_size_t, [_h]),
+    "imex_last_error": (ctypes.c_char_p, [_h]),
+    "imex_version": (ctypes.c_char_p, []),
+}
+
+_lib = None
+
+
+class ImexError(RuntimeError):
+    """A non-zero status from the C ABI, with the library's message."""
+
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+def load(path: str | None = None):
+    """Load the shared library (once) and declare every signature."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB
+    if not os.path.exists(p):
+        raise ImportError(f"{p} is missing: build it with `python -m imexlbm_gb300.build` "
+                          "(or __graft_entry__.build()); imexlbm_gb300 has no CPU fallback")
+    L = ctypes.CDLL(p)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = L
+    return L
+
+
+def check(rc: int, handle=None) -> None:
+    if rc != IMEX_OK:
+        msg = load().imex_last_error(handle)
+        raise ImexError(rc, msg.decode() if msg else "")

@@ -1,0 +1,416 @@
+// C ABI of one resident lattice (include/imexlbm.h).
+//
+// State machine.  The reference's step is Collision() then Streaming()
+// (src/main.cpp:43,61).  The fast kernel here is the fused "pull, then
+// collide" K = C(S(.)), so the handle keeps its distributions in one of two
+// states:
+//   kExact          the device buffer IS the reference's f;
+//   kPendingStream  the reference's f is S(buffer): the streaming of the last
+//                   step has not been applied yet.
+// Transitions (each keeps the reference's meaning for any call sequence):
+//   Collision  kExact -> collide in place            -> kExact
+//              kPending -> fused K into the other buffer -> kExact
+//   Streaming  kExact -> nothing (mark)               -> kPending
+//              kPending -> stream into the other buffer -> kPending
+// In the steady state Collision launches one fused kernel and Streaming
+// launches none.  Readers (Conserved, macroscopic, get_f) pull through S
+// when the state is kPending.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "imexlbm.h"
+#include "imexlbm_internal.hpp"
+#include "kernels_f64.cuh"
+#include "kernels_fx.cuh"
+
+namespace imex {
+
+static thread_local std::string g_thread_err;
+
+int set_thread_error(int code, const std::string& msg)
+{
+    g_thread_err = msg;
+    return code;
+}
+
+const char* thread_error() { return g_thread_err.c_str(); }
+
+}  // namespace imex
+
+using namespace imex;
+
+enum Tag { kUninit = 0, kExact = 1, kPendingStream = 2 };
+
+struct imex_lattice {
+    Geom g{};
+    size_t ncells = 0;
+    double tau0 = 0, rho0 = 0, u0 = 0;
+    int precision = IMEX_F64;
+    int engine = IMEX_ENGINE_AUTO;
+    void* buf[2] = {nullptr, nullptr};
+    int cur = 0;
+    Tag tag = kUninit;
+    int64_t steps = 0;
+    int64_t launches = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    int device = 0;
+    double* d_partial = nullptr;  // conserved partials (5 per block)
+    double* d_out = nullptr;      // 5 reduced values
+    double* h_out = nullptr;      // pinned copy of d_out
+    unsigned long long* d_fallback = nullptr;  // fixed-point engine fallback counter
+    size_t bytes = 0;
+    CollideF64 cf64{};
+    FxParams fx{};
+    bool fx_ok = false;  // fixed-point engine usable for this lattice
+    std::string err;
+};
+
+namespace {
+
+int fail(imex_lattice* h, int code, const std::string& msg)
+{
+    if (h) h->err = msg;
+    set_thread_error(code, msg);
+    return code;
+}
+
+int cuda_fail(imex_lattice* h, cudaError_t e, const char* what)
+{
+    cudaGetLastError();  // clear a non-sticky error
+    return fail(h, IMEX_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define IMEX_CUDA(h, call, what)                           \
+    do {                                                   \
+        cudaError_t e_ = (call);                           \
+        if (e_ != cudaSuccess) return cuda_fail(h, e_, what); \
+    } while (0)
+
+size_t elem_size(int precision) { return precision == IMEX_F64 ? 8 : precision == IMEX_F32 ? 4 : 2; }
+
+bool use_fixed(const imex_lattice* h)
+{
+    return h->precision == IMEX_F64 && h->fx_ok &&
+           (h->engine == IMEX_ENGINE_FIXED || h->engine == IMEX_ENGINE_AUTO);
+}
+
+double* dbuf(imex_lattice* h, int which) { return static_cast<double*>(h->buf[which]); }
+
+// One step-kernel launch in `mode` from buf[cur] into buf[cur] (collide) or
+// buf[1 - cur] (fused / stream).
+int launch_mode(imex_lattice* h, int mode)
+{
+    const double* src = dbuf(h, h->cur);
+    double* dst = mode == kModeCollide ? dbuf(h, h->cur) : dbuf(h, 1 - h->cur);
+    cudaError_t e;
+    if (mode != kModeStream && use_fixed(h))
+        e = launch_step_fx(mode, src, dst, h->g, h->fx, h->cf64, h->d_fallback, h->stream);
+    else
+        e = launch_step_f64(mode, src, dst, h->g, h->cf64, h->stream);
+    if (e != cudaSuccess) return cuda_fail(h, e, "step kernel launch");
+    ++h->launches;
+    if (mode != kModeCollide) h->cur = 1 - h->cur;
+    return IMEX_OK;
+}
+
+int check_ready(imex_lattice* h, const char* what)
+{
+    if (!h) return set_thread_error(IMEX_ERR_ARG, std::string(what) + ": null handle");
+    if (h->tag == kUninit) return fail(h, IMEX_ERR_STATE, std::string(what) + ": lattice not initialised");
+    IMEX_CUDA(h, cudaSetDevice(h->device), "cudaSetDevice");
+    return IMEX_OK;
+}
+
+// Make the device buffer hold the reference's f exactly (apply a pending
+// streaming into the other buffer).
+int materialize(imex_lattice* h)
+{
+    if (h->tag != kPendingStream) return IMEX_OK;
+    int rc = launch_mode(h, kModeStream);
+    if (rc) return rc;
+    h->tag = kExact;
+    return IMEX_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* imex_version(void) { return "imexlbm-gb300 0.1"; }
+
+const char* imex_last_error(const imex_lattice* h) { return h ? h->err.c_str() : thread_error(); }
+
+int imex_create(int nx, int ny, int nz, double tau, double rho0, double u0, int precision, imex_lattice** out)
+{
+    if (!out) return set_thread_error(IMEX_ERR_ARG, "imex_create: null output pointer");
+    *out = nullptr;
+    if (nx < 1 || ny < 1 || nz < 1) return set_thread_error(IMEX_ERR_ARG, "imex_create: lattice sizes must be >= 1");
+    if ((long long)ny * nx > 2147483647LL || nx > 65535 || ny > 65535)
+        return set_thread_error(IMEX_ERR_ARG, "imex_create: nx and ny must be <= 65535");
+    if (!std::isfinite(tau) || !std::isfinite(rho0) || !std::isfinite(u0) || !(tau + 0.5 > 0.0))
+        return set_thread_error(IMEX_ERR_ARG, "imex_create: tau, rho0, u0 must be finite with tau > -0.5");
+    if (precision != IMEX_F64)
+        return set_thread_error(IMEX_ERR_ARG, "imex_create: only IMEX_F64 storage is available in this build");
+
+    imex_lattice* h = new (std::nothrow) imex_lattice();
+    if (!h) return set_thread_error(IMEX_ERR_MEMORY, "imex_create: host allocation failed");
+    h->g.nx = nx;
+    h->g.ny = ny;
+    h->g.nz = nz;
+    h->ncells = (size_t)nx * ny * nz;
+    h->g.plane = h->ncells;
+    h->tau0 = tau;
+    h->rho0 = rho0;
+    h->u0 = u0;
+    h->precision = precision;
+    h->cf64 = make_collide_f64(tau);
+    h->fx_ok = make_fx_params(tau, rho0, &h->fx);
+
+    auto bail = [&](int code) {
+        imex_destroy(h);
+        return code;
+    };
+    cudaError_t e = cudaGetDevice(&h->device);
+    if (e != cudaSuccess) return bail(cuda_fail(nullptr, e, "cudaGetDevice"));
+
+    const size_t arr = (size_t)kQ * h->ncells * elem_size(precision);
+    const size_t nparts = conserved_partials(h->g);
+    const size_t need = 2 * arr + nparts * 5 * sizeof(double) + 64;
+    size_t free_b = 0, total_b = 0;
+    e = cudaMemGetInfo(&free_b, &total_b);
+    if (e != cudaSuccess) return bail(cuda_fail(nullptr, e, "cudaMemGetInfo"));
+    if (need > free_b) {
+        char msg[160];
+        std::snprintf(msg, sizeof msg, "imex_create: needs %.3f GB of device memory, %.3f GB free", need / 1e9,
+                      free_b / 1e9);
+        return bail(set_thread_error(IMEX_ERR_MEMORY, msg));
+    }
+    for (int b = 0; b < 2; ++b) {
+        e = cudaMalloc(&h->buf[b], arr);
+        if (e != cudaSuccess) return bail(set_thread_error(IMEX_ERR_MEMORY, "imex_create: cudaMalloc of f failed"));
+    }
+    e = cudaMalloc(&h->d_partial, nparts * 5 * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&h->d_out, 5 * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&h->d_fallback, sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMallocHost(&h->h_out, 5 * sizeof(double));
+    if (e != cudaSuccess) return bail(set_thread_error(IMEX_ERR_MEMORY, "imex_create: scratch allocation failed"));
+    e = cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return bail(cuda_fail(nullptr, e, "cudaStreamCreate"));
+    h->stream = h->own_stream;
+    e = cudaMemsetAsync(h->d_fallback, 0, sizeof(unsigned long long), h->stream);
+    if (e != cudaSuccess) return bail(cuda_fail(nullptr, e, "cudaMemset"));
+    h->bytes = 2 * arr + nparts * 5 * sizeof(double) + 5 * sizeof(double) + sizeof(unsigned long long);
+    *out = h;
+    return IMEX_OK;
+}
+
+void imex_destroy(imex_lattice* h)
+{
+    if (!h) return;
+    cudaSetDevice(h->device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    for (void* p : h->buf)
+        if (p) cudaFree(p);
+    if (h->d_partial) cudaFree(h->d_partial);
+    if (h->d_out) cudaFree(h->d_out);
+    if (h->d_fallback) cudaFree(h->d_fallback);
+    if (h->h_out) cudaFreeHost(h->h_out);
+    if (h->own_stream) cudaStreamDestroy(h->own_stream);
+    delete h;
+}
+
+int imex_initialize(imex_lattice* h)
+{
+    if (!h) return set_thread_error(IMEX_ERR_ARG, "imex_initialize: null handle");
+    IMEX_CUDA(h, cudaSetDevice(h->device), "cudaSetDevice");
+    // Per-axis trigonometric tables, src/lbm.cpp:81-93:
+    //   x = (double)(i - ghost + x_lo) / (double)glx * 2.0 * pi, pi = 3.1415926
+    const int n[3] = {h->g.nx, h->g.ny, h->g.nz};
+    const size_t tot = 3 * ((size_t)n[0] + n[1] + n[2]);
+    double* host = nullptr;
+    IMEX_CUDA(h, cudaMallocHost(&host, tot * sizeof(double)), "cudaMallocHost");
+    size_t off = 0;
+    size_t offs[3];
+    for (int d = 0; d < 3; ++d) {
+        offs[d] = off;
+        for (int i = 0; i < n[d]; ++i) {
+            const double xx = (double)i / (double)n[d] * 2.0 * 3.1415926;
+            host[off++] = std::sin(xx);
+            host[off++] = std::cos(xx);
+            host[off++] = std::cos(2.0 * xx);
+        }
+    }
+    double* dev = nullptr;
+    cudaError_t e = cudaMallocAsync(&dev, tot * sizeof(double), h->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dev, host, tot * sizeof(double), cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess)
+        e = launch_init_f64(dbuf(h, 0), h->g, dev + offs[0], dev + offs[1], dev + offs[2], h->rho0, h->u0, h->stream);
+    if (e == cudaSuccess) {
+        ++h->launches;
+        e = cudaFreeAsync(dev, h->stream);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    cudaFreeHost(host);
+    if (e != cudaSuccess) return cuda_fail(h, e, "imex_initialize");
+    h->cur = 0;
+    h->tag = kExact;
+    h->steps = 0;
+    return IMEX_OK;
+}
+
+int imex_collision(imex_lattice* h)
+{
+    int rc = check_ready(h, "imex_collision");
+    if (rc) return rc;
+    if (h->tag == kExact) return launch_mode(h, kModeCollide);
+    rc = launch_mode(h, kModeFused);
+    if (rc) return rc;
+    h->tag = kExact;
+    return IMEX_OK;
+}
+
+int imex_streaming(imex_lattice* h)
+{
+    int rc = check_ready(h, "imex_streaming");
+    if (rc) return rc;
+    if (h->tag == kPendingStream) {
+        rc = launch_mode(h, kModeStream);
+        if (rc) return rc;
+    }
+    h->tag = kPendingStream;
+    ++h->steps;
+    return IMEX_OK;
+}
+
+int imex_step(imex_lattice* h, int nsteps)
+{
+    if (nsteps < 0) return fail(h, IMEX_ERR_ARG, "imex_step: nsteps < 0");
+    for (int s = 0; s < nsteps; ++s) {
+        int rc = imex_collision(h);
+        if (rc) return rc;
+        rc = imex_streaming(h);
+        if (rc) return rc;
+    }
+    return check_ready(h, "imex_step");
+}
+
+int imex_conserved(imex_lattice* h, double out[5])
+{
+    int rc = check_ready(h, "imex_conserved");
+    if (rc) return rc;
+    if (!out) return fail(h, IMEX_ERR_ARG, "imex_conserved: null output");
+    const bool pull = h->tag == kPendingStream;
+    cudaError_t e = use_fixed(h) ? launch_conserved_fx(pull, dbuf(h, h->cur), h->g, h->fx, h->d_partial, h->d_out, h->stream)
+                                 : launch_conserved_f64(pull, dbuf(h, h->cur), h->g, h->d_partial, h->d_out, h->stream);
+    if (e != cudaSuccess) return cuda_fail(h, e, "conserved kernel launch");
+    h->launches += 2;
+    IMEX_CUDA(h, cudaMemcpyAsync(h->h_out, h->d_out, 5 * sizeof(double), cudaMemcpyDeviceToHost, h->stream), "cudaMemcpy");
+    IMEX_CUDA(h, cudaStreamSynchronize(h->stream), "imex_conserved");
+    bool finite = true;
+    for (int q = 0; q < 5; ++q) {
+        out[q] = h->h_out[q];
+        finite = finite && std::isfinite(out[q]);
+    }
+    if (!finite) return fail(h, IMEX_ERR_NONFINITE, "imex_conserved: non-finite diagnostics (the run diverged)");
+    return IMEX_OK;
+}
+
+int imex_macroscopic(imex_lattice* h, double* p, double* u, double* v, double* w)
+{
+    int rc = check_ready(h, "imex_macroscopic");
+    if (rc) return rc;
+    const size_t nb = h->ncells * sizeof(double);
+    double* d = nullptr;
+    IMEX_CUDA(h, cudaMallocAsync(&d, 4 * nb, h->stream), "cudaMallocAsync");
+    cudaError_t e = launch_macro_f64(h->tag == kPendingStream, dbuf(h, h->cur), h->g, d, d + h->ncells,
+                                     d + 2 * h->ncells, d + 3 * h->ncells, h->stream);
+    if (e == cudaSuccess) ++h->launches;
+    double* outs[4] = {p, u, v, w};
+    for (int q = 0; q < 4 && e == cudaSuccess; ++q)
+        if (outs[q]) e = cudaMemcpyAsync(outs[q], d + q * h->ncells, nb, cudaMemcpyDeviceToHost, h->stream);
+    cudaError_t e2 = cudaFreeAsync(d, h->stream);
+    if (e == cudaSuccess) e = e2;
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return cuda_fail(h, e, "imex_macroscopic");
+    return IMEX_OK;
+}
+
+static int get_f_impl(imex_lattice* h, double* dst, size_t n, cudaMemcpyKind kind, const char* what)
+{
+    int rc = check_ready(h, what);
+    if (rc) return rc;
+    if (!dst || n != (size_t)kQ * h->ncells) return fail(h, IMEX_ERR_ARG, std::string(what) + ": buffer size must be 27*nx*ny*nz");
+    rc = materialize(h);
+    if (rc) return rc;
+    IMEX_CUDA(h, cudaMemcpyAsync(dst, dbuf(h, h->cur), n * sizeof(double), kind, h->stream), what);
+    IMEX_CUDA(h, cudaStreamSynchronize(h->stream), what);
+    return IMEX_OK;
+}
+
+static int set_f_impl(imex_lattice* h, const double* src, size_t n, cudaMemcpyKind kind, const char* what)
+{
+    if (!h) return set_thread_error(IMEX_ERR_ARG, std::string(what) + ": null handle");
+    if (!src || n != (size_t)kQ * h->ncells) return fail(h, IMEX_ERR_ARG, std::string(what) + ": buffer size must be 27*nx*ny*nz");
+    IMEX_CUDA(h, cudaSetDevice(h->device), "cudaSetDevice");
+    IMEX_CUDA(h, cudaMemcpyAsync(dbuf(h, h->cur), src, n * sizeof(double), kind, h->stream), what);
+    IMEX_CUDA(h, cudaStreamSynchronize(h->stream), what);
+    h->tag = kExact;
+    return IMEX_OK;
+}
+
+int imex_get_f(imex_lattice* h, double* host, size_t n) { return get_f_impl(h, host, n, cudaMemcpyDeviceToHost, "imex_get_f"); }
+int imex_set_f(imex_lattice* h, const double* host, size_t n) { return set_f_impl(h, host, n, cudaMemcpyHostToDevice, "imex_set_f"); }
+int imex_get_f_device(imex_lattice* h, double* dev, size_t n)
+{
+    return get_f_impl(h, dev, n, cudaMemcpyDeviceToDevice, "imex_get_f_device");
+}
+int imex_set_f_device(imex_lattice* h, const double* dev, size_t n)
+{
+    return set_f_impl(h, dev, n, cudaMemcpyDeviceToDevice, "imex_set_f_device");
+}
+
+int imex_set_engine(imex_lattice* h, int engine)
+{
+    if (!h) return set_thread_error(IMEX_ERR_ARG, "imex_set_engine: null handle");
+    if (engine != IMEX_ENGINE_AUTO && engine != IMEX_ENGINE_NATIVE && engine != IMEX_ENGINE_FIXED)
+        return fail(h, IMEX_ERR_ARG, "imex_set_engine: unknown engine");
+    if (engine == IMEX_ENGINE_FIXED && !h->fx_ok)
+        return fail(h, IMEX_ERR_ARG, "imex_set_engine: fixed-point engine unavailable for these tau/rho0");
+    h->engine = engine;
+    return IMEX_OK;
+}
+
+int imex_set_stream(imex_lattice* h, void* s)
+{
+    if (!h) return set_thread_error(IMEX_ERR_ARG, "imex_set_stream: null handle");
+    h->stream = s ? static_cast<cudaStream_t>(s) : h->own_stream;
+    return IMEX_OK;
+}
+
+int imex_synchronize(imex_lattice* h)
+{
+    if (!h) return set_thread_error(IMEX_ERR_ARG, "imex_synchronize: null handle");
+    IMEX_CUDA(h, cudaStreamSynchronize(h->stream), "imex_synchronize");
+    return IMEX_OK;
+}
+
+int64_t imex_steps_done(const imex_lattice* h) { return h ? h->steps : -1; }
+int64_t imex_kernel_launches(const imex_lattice* h) { return h ? h->launches : -1; }
+size_t imex_device_bytes(const imex_lattice* h) { return h ? h->bytes : 0; }
+
+int imex_fallback_cells(imex_lattice* h, int64_t* out, int reset)
+{
+    if (!h || !out) return set_thread_error(IMEX_ERR_ARG, "imex_fallback_cells: null argument");
+    unsigned long long v = 0;
+    IMEX_CUDA(h, cudaMemcpyAsync(&v, h->d_fallback, sizeof v, cudaMemcpyDeviceToHost, h->stream), "cudaMemcpy");
+    IMEX_CUDA(h, cudaStreamSynchronize(h->stream), "imex_fallback_cells");
+    if (reset) IMEX_CUDA(h, cudaMemsetAsync(h->d_fallback, 0, sizeof v, h->stream), "cudaMemset");
+    *out = (int64_t)v;
+    return IMEX_OK;
+}
+
+}  // extern "C"

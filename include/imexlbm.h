@@ -1,0 +1,159 @@
+/*
+ * imexlbm.h - C ABI of the GB300-native IMEXLBM time step.
+ *
+ * One handle = one periodic D3Q27 lattice resident on one GPU.  The entry
+ * points mirror the reference's single-rank call surface (struct LBM and
+ * class System in Maccchiatooo/IMEXLBM); each declaration names the
+ * reference interface it replaces as path:line within that project.
+ *
+ * Conventions
+ *   - Every call returns an int status: IMEX_OK (0) or an IMEX_ERR_* code;
+ *     imex_last_error(h) gives a one-line description for the handle.
+ *   - The handle owns its device memory.  Calls on one handle are not
+ *     thread-safe; separate handles may be driven from separate threads.
+ *   - Work is queued on the handle's CUDA stream (default: a stream the
+ *     handle creates).  Calls that return host data synchronise that stream.
+ *   - Distribution arrays crossing the ABI are float64 in the reference's
+ *     index order f[a][x][y][z] (z fastest), interior cells only: 27*nx*ny*nz
+ *     values, a in the reference's direction order (src/lbm.cpp:20-30).
+ */
+#ifndef IMEXLBM_H
+#define IMEXLBM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define IMEX_OK 0
+#define IMEX_ERR_ARG 1       /* bad argument (null pointer, size, enum)            */
+#define IMEX_ERR_CUDA 2      /* a CUDA runtime call failed                          */
+#define IMEX_ERR_MEMORY 3    /* device allocation failed or over the HBM budget     */
+#define IMEX_ERR_DECK 4      /* input deck missing or malformed                     */
+#define IMEX_ERR_NONFINITE 5 /* diagnostics produced NaN or Inf                     */
+#define IMEX_ERR_STATE 6     /* call out of sequence (e.g. step before initialize)  */
+
+/* Storage precision of the distributions. */
+#define IMEX_F64 0    /* float64 storage (the reference's own precision)        */
+#define IMEX_F32 1    /* float32 storage, float32 collision                     */
+#define IMEX_F16DEV 2 /* float16 storage of f_a - w_a, float32 collision        */
+
+/* Arithmetic engine of the float64 collision. */
+#define IMEX_ENGINE_AUTO 0   /* fastest engine that meets float64 parity            */
+#define IMEX_ENGINE_NATIVE 1 /* native float64 FMA arithmetic                       */
+#define IMEX_ENGINE_FIXED 2  /* exact 64-bit fixed-point arithmetic on the integer
+                                pipes, rounded once to float64 per output          */
+
+typedef struct imex_lattice imex_lattice;
+
+/* Input deck: the nine numbers of input.in plus the derived quantities.
+ * Field names and meanings follow class System (src/System.hpp:11-19). */
+typedef struct imex_deck {
+    double rho0, R, u0;
+    int Re, Time, inter, sx, sy, sz;
+    double cs2, cs, Ma, miu, tau;
+} imex_deck;
+
+/* ---------------------------------------------------------------- deck -- */
+
+/* Parse deck text (nine whitespace-separated numbers; anything after the
+ * ninth is ignored) and derive cs2, cs, Ma, miu, tau.
+ * Replaces System::System() (src/System.cpp:11-29), which reads the same
+ * fields with std::istream >> in the same order.  Where the reference aborts
+ * on a missing or unreadable deck, this returns IMEX_ERR_DECK. */
+int imex_deck_parse(const char *text, imex_deck *out);
+
+/* Read and parse a deck file (System.cpp:16-24 reads "input.in" from CWD). */
+int imex_deck_read(const char *path, imex_deck *out);
+
+/* -------------------------------------------------------------- lattice -- */
+
+/* Create a lattice handle and allocate its device arrays.
+ * Replaces LBM::LBM(comm, sx, sy, sz, tau, rho0, u0) (src/lbm.hpp:179-183)
+ * plus the allocations of LBM::Initialize (src/lbm.cpp:43-57).
+ * precision: IMEX_F64 | IMEX_F32 | IMEX_F16DEV. */
+int imex_create(int nx, int ny, int nz, double tau, double rho0, double u0,
+                int precision, imex_lattice **out);
+
+/* Free the handle and its device memory.  Safe on NULL. */
+void imex_destroy(imex_lattice *h);
+
+/* Taylor-Green initial field and equilibrium distributions.
+ * Replaces LBM::Initialize() (src/lbm.cpp:38-111). */
+int imex_initialize(imex_lattice *h);
+
+/* BGK collision with relaxation rate 1/(tau0 + 0.5).
+ * Replaces LBM::Collision() (src/lbm.cpp:131-166). */
+int imex_collision(imex_lattice *h);
+
+/* Periodic pull streaming.
+ * Replaces LBM::Streaming() (src/lbm.cpp:168-207) including passf()
+ * (src/mpi_view_transfer.cpp:451-456), whose one-rank halo is the periodic
+ * image.  A Collision() followed by Streaming() runs as one fused
+ * collide + pull-stream kernel; either call alone keeps its own meaning. */
+int imex_streaming(imex_lattice *h);
+
+/* Advance nsteps reference steps (Collision then Streaming, repeated).
+ * Equivalent to the loop body of src/main.cpp:31-61 without reporting. */
+int imex_step(imex_lattice *h, int nsteps);
+
+/* Global diagnostics of the current distributions: out = {mass, px, py, pz,
+ * ke}.  Replaces LBM::Conserved() (src/lbm.cpp:266-306); synchronises.
+ * Returns IMEX_ERR_NONFINITE (with out filled) if any value is NaN or Inf. */
+int imex_conserved(imex_lattice *h, double out[5]);
+
+/* Per-cell macroscopic fields p = sum f / 3 and (u, v, w) = sum f e, each
+ * nx*ny*nz float64 on the host.  Replaces LBM::ComputeMacroscopic()
+ * (src/lbm.cpp:213-240).  Any output pointer may be NULL. */
+int imex_macroscopic(imex_lattice *h, double *p, double *u, double *v, double *w);
+
+/* Copy the current distributions (reference order, float64) to the host
+ * buffer of n = 27*nx*ny*nz values.  The reference exposes them as the
+ * public member LBM::f (src/lbm.hpp:165).  Synchronises. */
+int imex_get_f(imex_lattice *h, double *host, size_t n);
+
+/* Overwrite the distributions from a host buffer of n = 27*nx*ny*nz
+ * float64 values (reference order).  Marks the handle initialised. */
+int imex_set_f(imex_lattice *h, const double *host, size_t n);
+
+/* Same as imex_get_f / imex_set_f for a buffer already on this GPU. */
+int imex_get_f_device(imex_lattice *h, double *dev, size_t n);
+int imex_set_f_device(imex_lattice *h, const double *dev, size_t n);
+
+/* Select the float64 arithmetic engine (IMEX_ENGINE_*).  Default AUTO. */
+int imex_set_engine(imex_lattice *h, int engine);
+
+/* Queue the handle's work on an existing CUDA stream (cudaStream_t passed as
+ * void*; NULL restores the handle's own stream). */
+int imex_set_stream(imex_lattice *h, void *cuda_stream);
+
+/* Wait for the handle's queued work (Kokkos::fence() in the reference). */
+int imex_synchronize(imex_lattice *h);
+
+/* Reference steps completed since initialisation. */
+int64_t imex_steps_done(const imex_lattice *h);
+
+/* Kernel launches queued by this handle since creation (all kernels). */
+int64_t imex_kernel_launches(const imex_lattice *h);
+
+/* Cells whose float64 collision left the fixed-point engine's exact range
+ * and ran through the native float64 path instead, summed over all steps
+ * since the last reset; 0 for other engines.  Synchronises. */
+int imex_fallback_cells(imex_lattice *h, int64_t *out, int reset);
+
+/* Device bytes held by the handle. */
+size_t imex_device_bytes(const imex_lattice *h);
+
+/* Last error message of the handle (or of the calling thread when h is
+ * NULL, for errors raised before a handle exists).  Never NULL. */
+const char *imex_last_error(const imex_lattice *h);
+
+/* Library version string. */
+const char *imex_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* IMEXLBM_H */

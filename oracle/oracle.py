@@ -1,0 +1,139 @@
+"""ctypes wrapper around the CPU oracle (test infrastructure only).
+
+The oracle is the checker for the CUDA library: tests, the smoke check and the
+benchmark's CPU-baseline leg may call it; the product path never does.  It
+restates the reference's single-rank IMEXLBM step in plain C (see the header
+of ``lbm_oracle.c`` for the reference file:line of every function).
+
+Arrays are numpy float64 in the layout ``f[27][nx][ny][nz]`` (z fastest).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+Q = 27
+
+_lib = None
+
+
+class Deck(ctypes.Structure):
+    _fields_ = [
+        ("rho0", ctypes.c_double), ("R", ctypes.c_double), ("u0", ctypes.c_double),
+        ("Re", ctypes.c_int), ("Time", ctypes.c_int), ("inter", ctypes.c_int),
+        ("sx", ctypes.c_int), ("sy", ctypes.c_int), ("sz", ctypes.c_int),
+        ("cs2", ctypes.c_double), ("cs", ctypes.c_double), ("Ma", ctypes.c_double),
+        ("miu", ctypes.c_double), ("tau", ctypes.c_double),
+    ]
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle with its Makefile (gcc, OpenMP) if needed."""
+    src = os.path.join(HERE, "lbm_oracle.c")
+    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(src):
+        subprocess.run(["make", "-s", "-C", HERE], check=True)
+    return LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB_PATH)
+        dp = ctypes.POINTER(ctypes.c_double)
+        i = ctypes.c_int
+        L.oracle_set_threads.argtypes = [i]
+        L.oracle_max_threads.restype = i
+        L.oracle_weight.argtypes = [i]
+        L.oracle_weight.restype = ctypes.c_double
+        L.oracle_velocity.argtypes = [i, i]
+        L.oracle_velocity.restype = i
+        L.oracle_deck_parse.argtypes = [ctypes.c_char_p, ctypes.POINTER(Deck)]
+        L.oracle_deck_parse.restype = i
+        L.oracle_init.argtypes = [i, i, i, ctypes.c_double, ctypes.c_double, dp]
+        L.oracle_collide.argtypes = [i, i, i, ctypes.c_double, dp]
+        L.oracle_stream.argtypes = [i, i, i, dp, dp]
+        L.oracle_step.argtypes = [i, i, i, ctypes.c_double, dp, dp, i]
+        L.oracle_step_pingpong.argtypes = [i, i, i, ctypes.c_double, dp, dp]
+        L.oracle_conserved.argtypes = [i, i, i, dp, dp]
+        L.oracle_macroscopic.argtypes = [i, i, i, dp, dp, dp, dp, dp]
+        _lib = L
+    return _lib
+
+
+def _p(a: np.ndarray):
+    assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def set_threads(n: int) -> None:
+    lib().oracle_set_threads(int(n))
+
+
+def max_threads() -> int:
+    return int(lib().oracle_max_threads())
+
+
+def weights() -> np.ndarray:
+    return np.array([lib().oracle_weight(a) for a in range(Q)])
+
+
+def velocities() -> np.ndarray:
+    return np.array([[lib().oracle_velocity(a, d) for d in range(3)] for a in range(Q)], dtype=np.int64)
+
+
+def parse_deck(text: str) -> Deck:
+    d = Deck()
+    if lib().oracle_deck_parse(text.encode(), ctypes.byref(d)) != 0:
+        raise ValueError("malformed deck")
+    return d
+
+
+def init(nx: int, ny: int, nz: int, rho0: float, u0: float) -> np.ndarray:
+    f = np.empty((Q, nx, ny, nz), dtype=np.float64)
+    lib().oracle_init(nx, ny, nz, rho0, u0, _p(f))
+    return f
+
+
+def collide(f: np.ndarray, tau0: float) -> None:
+    _, nx, ny, nz = f.shape
+    lib().oracle_collide(nx, ny, nz, tau0, _p(f))
+
+
+def stream(f: np.ndarray) -> np.ndarray:
+    _, nx, ny, nz = f.shape
+    ft = np.empty_like(f)
+    lib().oracle_stream(nx, ny, nz, _p(f), _p(ft))
+    return ft
+
+
+def step(f: np.ndarray, tau0: float, nsteps: int = 1, scratch: np.ndarray | None = None) -> None:
+    """Advance f in place by nsteps reference steps (collide, stream, swap)."""
+    _, nx, ny, nz = f.shape
+    ft = np.empty_like(f) if scratch is None else scratch
+    lib().oracle_step(nx, ny, nz, tau0, _p(f), _p(ft), int(nsteps))
+
+
+def step_pingpong(f: np.ndarray, ft: np.ndarray, tau0: float) -> None:
+    """One step, collide f in place then stream into ft (no copy back)."""
+    _, nx, ny, nz = f.shape
+    lib().oracle_step_pingpong(nx, ny, nz, tau0, _p(f), _p(ft))
+
+
+def conserved(f: np.ndarray) -> np.ndarray:
+    _, nx, ny, nz = f.shape
+    out = np.zeros(5)
+    lib().oracle_conserved(nx, ny, nz, _p(f), _p(out))
+    return out
+
+
+def macroscopic(f: np.ndarray):
+    _, nx, ny, nz = f.shape
+    p, u, v, w = (np.empty((nx, ny, nz)) for _ in range(4))
+    lib().oracle_macroscopic(nx, ny, nz, _p(f), _p(p), _p(u), _p(v), _p(w))
+    return p, u, v, w

@@ -1,0 +1,187 @@
+"""GPU parity of the CUDA path against the CPU oracle, through the C ABI.
+
+Tolerance: every f_a of every cell within 1e-12 relative of the oracle
+(|gpu - oracle| <= 1e-12 * |oracle|), the bound the reference's single-rank
+run must meet; reductions within 1e-12 relative (mass, ke) and momentum
+within the regression's absolute 1e-10.  Streaming alone is a permutation
+and must be bit-identical.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-12
+ENGINES = ["native", "fixed"]
+
+
+def rel_err(a, b):
+    return float(np.max(np.abs(a - b) / np.abs(b)))
+
+
+def engine_id(imex, name):
+    return {"native": imex.IMEX_ENGINE_NATIVE, "fixed": imex.IMEX_ENGINE_FIXED}[name]
+
+
+def make(imex, shape, tau, rho0=1.0, u0=0.05, engine="native"):
+    lat = imex.LBM(*shape, tau, rho0, u0)
+    try:
+        lat.set_engine(engine_id(imex, engine))
+    except imex.ImexError:
+        lat.close()
+        pytest.skip(f"{engine} engine not available in this build")
+    return lat
+
+
+def test_init_matches_oracle(imex, oracle):
+    for shape in [(16, 16, 16), (17, 19, 23), (1, 1, 8), (3, 2, 1)]:
+        with imex.LBM(*shape, 0.01, 1.0, 0.05) as lat:
+            lat.Initialize()
+            got = lat.get_f()
+        want = oracle.init(*shape, 1.0, 0.05)
+        assert np.array_equal(got, want), shape
+
+
+@pytest.mark.parametrize("engine", ENGINES)
+def test_regression_deck_32cubed_100_steps(imex, oracle, engine):
+    """The 32^3 deck rho0=1, Re=1600, u0=0.05: 100 steps, report every 10.
+    Conserved at every report step (steady-state fused path, no
+    materialisation), all f_a at step 100."""
+    d = oracle.parse_deck("1.0 0.1 1600\n0.05 100 10\n32 32 32\n")
+    lat = make(imex, (32, 32, 32), d.tau, engine=engine)
+    lat.Initialize()
+    f = oracle.init(32, 32, 32, d.rho0, d.u0)
+    for it in range(1, 101):
+        lat.Collision()
+        lat.Streaming()
+        oracle.step(f, d.tau, 1)
+        if it % 10 == 0:
+            c = np.array(lat.Conserved())
+            w = oracle.conserved(f)
+            assert abs(c[0] - w[0]) <= RTOL * abs(w[0])
+            assert abs(c[4] - w[4]) <= RTOL * abs(w[4])
+            assert np.abs(c[1:4]).max() <= 1e-10
+    got = lat.get_f()
+    assert rel_err(got, f) <= RTOL
+    assert lat.steps_done() == 100
+    lat.close()
+
+
+@pytest.mark.parametrize("engine", ENGINES)
+def test_every_f_at_every_report_step(imex, oracle, engine):
+    """get_f at each report step (materialises the pending streaming)."""
+    d = oracle.parse_deck("1.0 0.1 1600\n0.05 100 10\n32 32 32\n")
+    lat = make(imex, (32, 32, 32), d.tau, engine=engine)
+    lat.Initialize()
+    f = oracle.init(32, 32, 32, d.rho0, d.u0)
+    worst = 0.0
+    for it in range(10, 101, 10):
+        lat.step(10)
+        oracle.step(f, d.tau, 10)
+        worst = max(worst, rel_err(lat.get_f(), f))
+    assert worst <= RTOL, worst
+    lat.close()
+
+
+@pytest.mark.parametrize("engine", ENGINES)
+@pytest.mark.parametrize("shape", [(17, 19, 23), (8, 8, 8), (1, 1, 16), (2, 3, 5), (40, 1, 33), (5, 64, 2)])
+def test_ragged_shapes(imex, oracle, shape, engine):
+    tau = 0.02
+    lat = make(imex, shape, tau, u0=0.06, engine=engine)
+    lat.Initialize()
+    f = oracle.init(*shape, 1.0, 0.06)
+    lat.step(7)
+    oracle.step(f, tau, 7)
+    assert rel_err(lat.get_f(), f) <= RTOL
+    c = np.array(lat.Conserved())
+    w = oracle.conserved(f)
+    assert abs(c[0] - w[0]) <= RTOL * abs(w[0])
+    assert abs(c[4] - w[4]) <= 1e-11 * abs(w[4])
+    lat.close()
+
+
+def test_streaming_alone_is_bitwise(imex, oracle):
+    rng = np.random.default_rng(3)
+    shape = (9, 7, 12)
+    f = rng.random((27,) + shape)
+    with imex.LBM(*shape, 0.05, 1.0, 0.05) as lat:
+        lat.set_f(f)
+        lat.Streaming()
+        lat.Streaming()
+        got = lat.get_f()
+    assert np.array_equal(got, oracle.stream(oracle.stream(f)))
+
+
+@pytest.mark.parametrize("engine", ENGINES)
+def test_call_sequences(imex, oracle, engine):
+    """Any order of Collision/Streaming keeps the reference's meaning."""
+    shape = (10, 12, 14)
+    tau = 0.05
+    seq = "CSCSSCCSCSCCSS"
+    lat = make(imex, shape, tau, engine=engine)
+    lat.Initialize()
+    f = oracle.init(*shape, 1.0, 0.05)
+    for op in seq:
+        if op == "C":
+            lat.Collision()
+            oracle.collide(f, tau)
+        else:
+            lat.Streaming()
+            f = oracle.stream(f)
+    assert rel_err(lat.get_f(), f) <= RTOL
+    lat.close()
+
+
+def test_macroscopic(imex, oracle):
+    shape = (12, 10, 16)
+    tau = 0.01
+    with imex.LBM(*shape, tau, 1.0, 0.05) as lat:
+        lat.Initialize()
+        lat.step(5)
+        p, u, v, w = lat.ComputeMacroscopic()
+    f = oracle.init(*shape, 1.0, 0.05)
+    oracle.step(f, tau, 5)
+    for got, want in zip((p, u, v, w), oracle.macroscopic(f)):
+        assert np.max(np.abs(got - want)) <= 1e-13
+
+
+def test_set_get_roundtrip_and_restart(imex, oracle):
+    """Checkpoint f, continue, restore, continue again: same answer."""
+    shape = (16, 8, 12)
+    tau = 0.02
+    with imex.LBM(*shape, tau, 1.0, 0.05) as lat:
+        lat.Initialize()
+        lat.step(4)
+        ck = lat.get_f()
+        lat.step(6)
+        a = lat.get_f()
+        lat.set_f(ck)
+        lat.step(6)
+        b = lat.get_f()
+    assert np.array_equal(a, b)
+
+
+def test_nonfinite_is_reported(imex):
+    """A diverging request (Mach ~1.7) is reported by status, not a crash."""
+    with imex.LBM(16, 16, 16, 1e-4, 1.0, 1.0) as lat:
+        lat.Initialize()
+        status = None
+        for _ in range(60):
+            lat.step(10)
+            try:
+                lat.Conserved()
+            except imex.ImexError as e:
+                status = e.code
+                break
+        assert status == 5
+        vals = lat.Conserved(allow_nonfinite=True)
+        assert not all(np.isfinite(vals))
+
+
+def test_state_errors(imex):
+    with imex.LBM(4, 4, 4, 0.1, 1.0, 0.05) as lat:
+        with pytest.raises(imex.ImexError) as e:
+            lat.Collision()
+        assert e.value.code == 6
+        with pytest.raises(imex.ImexError):
+            lat.get_f(np.empty(10))
