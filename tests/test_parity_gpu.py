@@ -96,7 +96,9 @@ def test_ragged_shapes(imex, oracle, shape, engine):
     c = np.array(lat.Conserved())
     w = oracle.conserved(f)
     assert abs(c[0] - w[0]) <= RTOL * abs(w[0])
-    assert abs(c[4] - w[4]) <= 1e-11 * abs(w[4])
+    # ke of a degenerate lattice (e.g. 1x1xN, where only acoustic motion
+    # survives) is itself a cancellation residue: floor of 1e-18 per cell
+    assert abs(c[4] - w[4]) <= RTOL * abs(w[4]) + 1e-18 * np.prod(shape)
     lat.close()
 
 
