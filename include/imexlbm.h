@@ -122,6 +122,27 @@ int imex_set_f(imex_lattice *h, const double *host, size_t n);
 int imex_get_f_device(imex_lattice *h, double *dev, size_t n);
 int imex_set_f_device(imex_lattice *h, const double *dev, size_t n);
 
+/* Conserved diagnostics of distributions in a caller-owned device buffer,
+ * without allocating anything.  No counterpart in the reference: it is for
+ * callers that cannot call cudaMalloc - a host code whose device memory is
+ * owned by its own pool allocator, or a latency-critical loop where
+ * cudaMalloc's implicit device synchronisation is not acceptable.
+ *   f_dev    27*nx*ny*nz float64 in the layout above, on the current device
+ *   out_dev  5 float64 on the current device: {mass, px, py, pz, ke}, as
+ *            imex_conserved computes them
+ *   stream   cudaStream_t as void* (NULL: the legacy default stream); the
+ *            call is asynchronous on it
+ * Scratch: a file-scope static device array of 131072 partial sums (5 MiB),
+ * which every GPU that loads this library holds until the process exits.
+ * Lattices needing more partial sums than that (one per 128 z-cells of a
+ * row, e.g. more than 256x256x256) are rejected with IMEX_ERR_ARG.  The
+ * first call on each device looks the array's device address up
+ * (cudaGetSymbolAddress), so make that first call before any stream
+ * capture.  All calls share the array: calls that overlap on the GPU (on
+ * different streams, or from different threads) race; serialise them.
+ * Errors are reported through imex_last_error(NULL). */
+int imex_conserved_noalloc(const double *f_dev, int nx, int ny, int nz, double *out_dev, void *stream);
+
 /* Select the float64 arithmetic engine (IMEX_ENGINE_*).  Default AUTO. */
 int imex_set_engine(imex_lattice *h, int engine);
 
