@@ -37,7 +37,8 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-BYTES_PER_CELL_F64 = 432  # 27 float64 read + 27 written per cell update
+# algorithmic bytes per cell update: 27 values read + 27 written
+BYTES_PER_CELL = {"f64": 432, "f32": 216, "f16dev": 108}
 FLOP_PER_CELL = 594       # the reference's own count (src/profile.cpp:38)
 DECK = "1.0 0.1 1600\n0.05 1000 100\n256 256 256\n"
 FALLBACK_HBM_GBS = 6800.0
@@ -50,6 +51,8 @@ def parse_args(argv=None):
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--engine", choices=["auto", "native", "fixed"], default="auto")
+    ap.add_argument("--precision", choices=["f64", "f32", "f16dev"], default="f64",
+                    help="storage precision (f64: the reference's; f32 / f16dev: the reduced-precision variants)")
     ap.add_argument("--size", type=int, default=256, help="cubic lattice edge (default: the shipped deck's 256)")
     ap.add_argument("--report-every", type=int, default=100)
     ap.add_argument("--no-e2e", action="store_true")
@@ -197,9 +200,13 @@ def parse_deck_text(n):
 
 
 def workload_config(a, engine):
-    return {"workload": f"taylor-green {a.size}^3 periodic D3Q27, Re=1600, u0=0.05, float64 distributions",
-            "grid": [a.size] * 3, "precision": "f64", "engine": engine, "report_every": a.report_every,
-            "l2": "inputs larger than L2 (2 arrays x %.2f GB), no flush" % (27 * a.size ** 3 * 8 / 1e9),
+    prec = getattr(a, "precision", "f64")
+    desc = {"f64": "float64 distributions", "f32": "float32 distributions",
+            "f16dev": "float16 deviations f - w"}[prec]
+    esize = {"f64": 8, "f32": 4, "f16dev": 2}[prec]
+    return {"workload": f"taylor-green {a.size}^3 periodic D3Q27, Re=1600, u0=0.05, {desc}",
+            "grid": [a.size] * 3, "precision": prec, "engine": engine, "report_every": a.report_every,
+            "l2": "inputs larger than L2 (2 arrays x %.2f GB), no flush" % (27 * a.size ** 3 * esize / 1e9),
             "parallelism": "replicas (one independent lattice per GPU)"}
 
 
@@ -220,11 +227,18 @@ def run_ours(a):
     n = a.size
     cells = n ** 3
     engine = {"auto": m.IMEX_ENGINE_AUTO, "native": m.IMEX_ENGINE_NATIVE, "fixed": m.IMEX_ENGINE_FIXED}[a.engine]
+    prec = {"f64": m.IMEX_F64, "f32": m.IMEX_F32, "f16dev": m.IMEX_F16DEV}[a.precision]
+    if prec != m.IMEX_F64:
+        engine = m.IMEX_ENGINE_AUTO
     stream = torch.cuda.Stream()
-    lat = m.LBM(n, n, n, d["tau"], d["rho0"], d["u0"], engine=engine)
+    lat = m.LBM(n, n, n, d["tau"], d["rho0"], d["u0"], precision=prec, engine=engine)
     lat.set_stream(stream.cuda_stream)
     lat.Initialize()
     eng_name = "fixed" if (engine == m.IMEX_ENGINE_FIXED) else "native" if engine == m.IMEX_ENGINE_NATIVE else "auto"
+    if prec != m.IMEX_F64:
+        eng_name = "float32"
+    elif engine == m.IMEX_ENGINE_AUTO:
+        eng_name = "fixed" if d["rho0"] >= 0.75 and d["rho0"] <= 1.25 else "native"
 
     def barrier():
         if world > 1:
@@ -262,20 +276,21 @@ def run_ours(a):
     # roofline of the fused step kernel: every timed launch is that kernel
     hbm, peak_kind = load_peaks()
     launch_ms = ms / max(1, gpu_launches)
-    achieved = BYTES_PER_CELL_F64 * cells / (launch_ms * 1e-3) / 1e9
-    kname = "step_fx" if eng_name != "native" else "step_f64"
+    bpc = BYTES_PER_CELL[a.precision]
+    achieved = bpc * cells / (launch_ms * 1e-3) / 1e9
+    kname = {"fixed": "step_fx", "native": "step_f64", "float32": "step_lowp_" + a.precision}[eng_name]
     tr = load_traffic(kname)
     roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
             "frac": round(achieved / hbm, 4), "peak_kind": peak_kind,
             "traffic": round(tr * cells, 0) if tr is not None else None,
-            "kernel": kname, "algorithmic_bytes_per_launch": BYTES_PER_CELL_F64 * cells}
+            "kernel": kname, "algorithmic_bytes_per_launch": bpc * cells}
 
     # end-to-end through the public API with host buffers
     e2e = None
     if not a.no_e2e:
         nval = 27 * cells
         host = torch.empty(nval, dtype=torch.float64, pin_memory=True)
-        lat2 = m.LBM(n, n, n, d["tau"], d["rho0"], d["u0"], engine=engine)
+        lat2 = m.LBM(n, n, n, d["tau"], d["rho0"], d["u0"], precision=prec, engine=engine)
         lat2.set_stream(stream.cuda_stream)
         lat2.Initialize()
         import ctypes
@@ -321,12 +336,13 @@ def run_ours(a):
         line = {"metric": "MLUPS", "value": round(value, 2), "unit": "MLUPS", "n_gpus": world, "steps": a.steps,
                 "warmup": max(3, a.warmup), "ms_per_step": round(t_max / a.steps, 4), "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None,
-                "dtype": "s64 fixed-point arithmetic, f64 storage" if eng_name != "native" else "f64",
+                "dtype": {"fixed": "s64 fixed-point arithmetic, f64 storage", "native": "f64",
+                          "float32": "f32 arithmetic, %s storage" % a.precision}[eng_name],
                 "data": "synthetic: Taylor-Green initial field (deterministic, no seed)",
                 "config": workload_config(a, eng_name), "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
                 "gpu_launches": gpu_launches, "clocks": clk.summary(),
                 "fallback_cells": fallback, "mass": cons[0], "ke": cons[4],
-                "roofline_glups_at_peak": round(hbm * 1e9 / BYTES_PER_CELL_F64 / 1e9, 3)}
+                "roofline_glups_at_peak": round(hbm / bpc, 3)}
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist

@@ -56,6 +56,7 @@ SIGNATURES = {
     "imex_step": (ctypes.c_int, [_h, ctypes.c_int]),
     "imex_conserved": (ctypes.c_int, [_h, _dp]),
     "imex_macroscopic": (ctypes.c_int, [_h, _dp, _dp, _dp, _dp]),
+    "imex_velocity_max_diff": (ctypes.c_int, [_h, _h, _dp]),
     "imex_get_f": (ctypes.c_int, [_h, _dp, ctypes.c_size_t]),
     "imex_set_f": (ctypes.c_int, [_h, _dp, ctypes.c_size_t]),
     "imex_get_f_device": (ctypes.c_int, [_h, ctypes.c_void_p, ctypes.c_size_t]),

@@ -53,6 +53,13 @@ struct PullIndex {
     {
         return (size_t)A * g.plane + row[ex(A, 0) + 1][ex(A, 1) + 1] + zk[ex(A, 2) + 1];
     }
+
+    // Same for a direction that is a compile-time constant only after
+    // unrolling.
+    __device__ __forceinline__ size_t at_dyn(const Geom& g, int a) const
+    {
+        return (size_t)a * g.plane + row[ex(a, 0) + 1][ex(a, 1) + 1] + zk[ex(a, 2) + 1];
+    }
 };
 
 template <int A, typename T>

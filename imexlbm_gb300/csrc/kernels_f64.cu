@@ -10,15 +10,11 @@
 // term and the weight, and the relaxation is one FMA per direction.
 #include "kernels_f64.cuh"
 #include "collide_f64.cuh"
+#include "tg_init.cuh"
 
 namespace imex {
 
 // ------------------------------------------------------------------- init --
-// Taylor-Green field and equilibrium, src/lbm.cpp:78-108.  The trigonometric
-// factors depend on one coordinate each and come in as per-axis tables
-// (sin, cos, cos 2x of x = i / n * 2 * 3.1415926), computed on the host with
-// the same expressions.  Products use round-to-nearest intrinsics so no FMA
-// contraction changes the reference's rounding.
 __global__ void __launch_bounds__(kStepBlock) k_init_f64(double* __restrict__ f, Geom g, const double* __restrict__ tx,
                                                          const double* __restrict__ ty, const double* __restrict__ tz,
                                                          double rho0, double u0)
@@ -26,27 +22,11 @@ __global__ void __launch_bounds__(kStepBlock) k_init_f64(double* __restrict__ f,
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y, i = blockIdx.z;
     if (k >= g.nz) return;
-    const double sx = tx[3 * i], cx = tx[3 * i + 1], c2x = tx[3 * i + 2];
-    const double sy = ty[3 * j], cy = ty[3 * j + 1], c2y = ty[3 * j + 2];
-    const double cz = tz[3 * k + 1], c2z = tz[3 * k + 2];
-    const double cs2 = 1.0 / 3.0;
-    const double u = __dmul_rn(__dmul_rn(__dmul_rn(u0, sx), cy), cz);
-    const double v = __dmul_rn(__dmul_rn(__dmul_rn(-u0, cx), sy), cz);
-    const double w = 0.0;
-    const double amp = __ddiv_rn(__dmul_rn(__dmul_rn(rho0, u0), u0), 16.0);
-    const double p = __dadd_rn(__dmul_rn(rho0, cs2), __dmul_rn(__dmul_rn(amp, __dadd_rn(c2x, c2y)), __dadd_rn(c2z, 2.0)));
-    const double udu = __dadd_rn(__dadd_rn(__dmul_rn(u, u), __dmul_rn(v, v)), __dmul_rn(w, w));
+    double fe[kQ];
+    tg_init_cell(fe, tx, ty, tz, i, j, k, rho0, u0);
     const size_t cell = ((size_t)i * g.ny + j) * g.nz + k;
 #pragma unroll
-    for (int a = 0; a < kQ; ++a) {
-        // e(a,0)*u + e(a,1)*v + e(a,2)*w with integer e, as written
-        const double edu = __dadd_rn(__dadd_rn(__dmul_rn((double)ex(a, 0), u), __dmul_rn((double)ex(a, 1), v)),
-                                     __dmul_rn((double)ex(a, 2), w));
-        const double br = __dsub_rn(__dadd_rn(__dadd_rn(__dmul_rn(3.0, p), __dmul_rn(3.0, edu)),
-                                              __dmul_rn(__dmul_rn(4.5, edu), edu)),
-                                    __dmul_rn(1.5, udu));
-        f[(size_t)a * g.plane + cell] = __dmul_rn(weight(a), br);
-    }
+    for (int a = 0; a < kQ; ++a) f[(size_t)a * g.plane + cell] = fe[a];
 }
 
 // ------------------------------------------------------------------- step --
@@ -155,10 +135,34 @@ __global__ void __launch_bounds__(kStepBlock) k_macro_f64(const double* __restri
     double pl, ul, vl, wl;
     moments_f64(f, pl, ul, vl, wl);
     const size_t cell = ((size_t)i * g.ny + j) * g.nz + k;
-    p[cell] = pl * (1.0 / 3.0);
+    if (p) p[cell] = pl * (1.0 / 3.0);
     u[cell] = ul;
     v[cell] = vl;
     w[cell] = wl;
+}
+
+// max over cells of |a - b| and of |b| for three component arrays of n
+// values; results as the bit patterns of non-negative doubles (ordered like
+// unsigned integers), combined with atomicMax.
+__global__ void k_maxdiff3(const double* __restrict__ a, const double* __restrict__ b, size_t n,
+                           unsigned long long* __restrict__ out)
+{
+    double md = 0.0, mb = 0.0;
+    for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            md = fmax(md, fabs(a[c * n + q] - b[c * n + q]));
+            mb = fmax(mb, fabs(b[c * n + q]));
+        }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        md = fmax(md, __shfl_down_sync(0xffffffffu, md, o));
+        mb = fmax(mb, __shfl_down_sync(0xffffffffu, mb, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMax(out, (unsigned long long)__double_as_longlong(md));
+        atomicMax(out + 1, (unsigned long long)__double_as_longlong(mb));
+    }
 }
 
 // ---------------------------------------------------------------- launchers --
@@ -196,7 +200,12 @@ cudaError_t launch_conserved_f64(bool pull, const double* src, const Geom& g, do
         k_conserved_f64<false><<<step_grid(g), kStepBlock, 0, s>>>(src, g, partial);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    k_reduce_partials<<<1, 1024, 0, s>>>(partial, conserved_partials(g), out);
+    return launch_reduce_partials(partial, conserved_partials(g), out, s);
+}
+
+cudaError_t launch_reduce_partials(const double* partial, size_t n, double* out, cudaStream_t s)
+{
+    k_reduce_partials<<<1, 1024, 0, s>>>(partial, n, out);
     return cudaGetLastError();
 }
 
@@ -207,6 +216,14 @@ cudaError_t launch_macro_f64(bool pull, const double* src, const Geom& g, double
         k_macro_f64<true><<<step_grid(g), kStepBlock, 0, s>>>(src, g, p, u, v, w);
     else
         k_macro_f64<false><<<step_grid(g), kStepBlock, 0, s>>>(src, g, p, u, v, w);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_maxdiff3(const double* a, const double* b, size_t n, unsigned long long* out, cudaStream_t s)
+{
+    cudaError_t e = cudaMemsetAsync(out, 0, 2 * sizeof(unsigned long long), s);
+    if (e != cudaSuccess) return e;
+    k_maxdiff3<<<152 * 8, 256, 0, s>>>(a, b, n, out);
     return cudaGetLastError();
 }
 

@@ -25,6 +25,7 @@
 #include "imexlbm_internal.hpp"
 #include "kernels_f64.cuh"
 #include "kernels_fx.cuh"
+#include "kernels_lowp.cuh"
 
 namespace imex {
 
@@ -64,6 +65,7 @@ struct imex_lattice {
     unsigned long long* d_fallback = nullptr;  // fixed-point engine fallback counter
     size_t bytes = 0;
     CollideF64 cf64{};
+    CollideF32 cf32{};
     FxParams fx{};
     bool fx_ok = false;  // fixed-point engine usable for this lattice
     std::string err;
@@ -100,6 +102,8 @@ bool use_fixed(const imex_lattice* h)
 
 double* dbuf(imex_lattice* h, int which) { return static_cast<double*>(h->buf[which]); }
 
+bool lowp(const imex_lattice* h) { return h->precision != IMEX_F64; }
+
 // One step-kernel launch in `mode` from buf[cur] into buf[cur] (collide) or
 // buf[1 - cur] (fused / stream).
 int launch_mode(imex_lattice* h, int mode)
@@ -107,7 +111,9 @@ int launch_mode(imex_lattice* h, int mode)
     const double* src = dbuf(h, h->cur);
     double* dst = mode == kModeCollide ? dbuf(h, h->cur) : dbuf(h, 1 - h->cur);
     cudaError_t e;
-    if (mode != kModeStream && use_fixed(h))
+    if (lowp(h))
+        e = launch_step_lowp(h->precision, mode, src, dst, h->g, h->cf32, h->stream);
+    else if (mode != kModeStream && use_fixed(h))
         e = launch_step_fx(mode, src, dst, h->g, h->fx, h->cf64, h->d_fallback, h->stream);
     else
         e = launch_step_f64(mode, src, dst, h->g, h->cf64, h->stream);
@@ -153,8 +159,8 @@ int imex_create(int nx, int ny, int nz, double tau, double rho0, double u0, int 
         return set_thread_error(IMEX_ERR_ARG, "imex_create: nx and ny must be <= 65535");
     if (!std::isfinite(tau) || !std::isfinite(rho0) || !std::isfinite(u0) || !(tau + 0.5 > 0.0))
         return set_thread_error(IMEX_ERR_ARG, "imex_create: tau, rho0, u0 must be finite with tau > -0.5");
-    if (precision != IMEX_F64)
-        return set_thread_error(IMEX_ERR_ARG, "imex_create: only IMEX_F64 storage is available in this build");
+    if (precision != IMEX_F64 && precision != IMEX_F32 && precision != IMEX_F16DEV)
+        return set_thread_error(IMEX_ERR_ARG, "imex_create: precision must be IMEX_F64, IMEX_F32 or IMEX_F16DEV");
 
     imex_lattice* h = new (std::nothrow) imex_lattice();
     if (!h) return set_thread_error(IMEX_ERR_MEMORY, "imex_create: host allocation failed");
@@ -168,6 +174,7 @@ int imex_create(int nx, int ny, int nz, double tau, double rho0, double u0, int 
     h->u0 = u0;
     h->precision = precision;
     h->cf64 = make_collide_f64(tau);
+    h->cf32 = make_collide_f32(tau);
     h->fx_ok = make_fx_params(tau, rho0, &h->fx);
 
     auto bail = [&](int code) {
@@ -248,7 +255,10 @@ int imex_initialize(imex_lattice* h)
     cudaError_t e = cudaMallocAsync(&dev, tot * sizeof(double), h->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(dev, host, tot * sizeof(double), cudaMemcpyHostToDevice, h->stream);
     if (e == cudaSuccess)
-        e = launch_init_f64(dbuf(h, 0), h->g, dev + offs[0], dev + offs[1], dev + offs[2], h->rho0, h->u0, h->stream);
+        e = lowp(h) ? launch_init_lowp(h->precision, h->buf[0], h->g, dev + offs[0], dev + offs[1], dev + offs[2], h->rho0,
+                                       h->u0, h->stream)
+                    : launch_init_f64(dbuf(h, 0), h->g, dev + offs[0], dev + offs[1], dev + offs[2], h->rho0, h->u0,
+                                      h->stream);
     if (e == cudaSuccess) {
         ++h->launches;
         e = cudaFreeAsync(dev, h->stream);
@@ -304,8 +314,10 @@ int imex_conserved(imex_lattice* h, double out[5])
     if (rc) return rc;
     if (!out) return fail(h, IMEX_ERR_ARG, "imex_conserved: null output");
     const bool pull = h->tag == kPendingStream;
-    cudaError_t e = use_fixed(h) ? launch_conserved_fx(pull, dbuf(h, h->cur), h->g, h->fx, h->d_partial, h->d_out, h->stream)
-                                 : launch_conserved_f64(pull, dbuf(h, h->cur), h->g, h->d_partial, h->d_out, h->stream);
+    cudaError_t e =
+        lowp(h) ? launch_conserved_lowp(h->precision, pull, h->buf[h->cur], h->g, h->d_partial, h->d_out, h->stream)
+        : use_fixed(h) ? launch_conserved_fx(pull, dbuf(h, h->cur), h->g, h->fx, h->d_partial, h->d_out, h->stream)
+                       : launch_conserved_f64(pull, dbuf(h, h->cur), h->g, h->d_partial, h->d_out, h->stream);
     if (e != cudaSuccess) return cuda_fail(h, e, "conserved kernel launch");
     h->launches += 2;
     IMEX_CUDA(h, cudaMemcpyAsync(h->h_out, h->d_out, 5 * sizeof(double), cudaMemcpyDeviceToHost, h->stream), "cudaMemcpy");
@@ -319,6 +331,26 @@ int imex_conserved(imex_lattice* h, double out[5])
     return IMEX_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+// Per-cell p (optional), u, v, w of the handle's current distributions into
+// device arrays of ncells doubles each, on the handle's stream.
+int macro_fields(imex_lattice* h, double* p, double* u, double* v, double* w)
+{
+    const bool pull = h->tag == kPendingStream;
+    cudaError_t e = lowp(h) ? launch_macro_lowp(h->precision, pull, h->buf[h->cur], h->g, p, u, v, w, h->stream)
+                            : launch_macro_f64(pull, dbuf(h, h->cur), h->g, p, u, v, w, h->stream);
+    if (e != cudaSuccess) return cuda_fail(h, e, "macroscopic kernel launch");
+    ++h->launches;
+    return IMEX_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
 int imex_macroscopic(imex_lattice* h, double* p, double* u, double* v, double* w)
 {
     int rc = check_ready(h, "imex_macroscopic");
@@ -326,16 +358,52 @@ int imex_macroscopic(imex_lattice* h, double* p, double* u, double* v, double* w
     const size_t nb = h->ncells * sizeof(double);
     double* d = nullptr;
     IMEX_CUDA(h, cudaMallocAsync(&d, 4 * nb, h->stream), "cudaMallocAsync");
-    cudaError_t e = launch_macro_f64(h->tag == kPendingStream, dbuf(h, h->cur), h->g, d, d + h->ncells,
-                                     d + 2 * h->ncells, d + 3 * h->ncells, h->stream);
-    if (e == cudaSuccess) ++h->launches;
+    rc = macro_fields(h, d, d + h->ncells, d + 2 * h->ncells, d + 3 * h->ncells);
+    cudaError_t e = cudaSuccess;
     double* outs[4] = {p, u, v, w};
-    for (int q = 0; q < 4 && e == cudaSuccess; ++q)
+    for (int q = 0; q < 4 && rc == IMEX_OK && e == cudaSuccess; ++q)
         if (outs[q]) e = cudaMemcpyAsync(outs[q], d + q * h->ncells, nb, cudaMemcpyDeviceToHost, h->stream);
     cudaError_t e2 = cudaFreeAsync(d, h->stream);
+    if (rc) return rc;
     if (e == cudaSuccess) e = e2;
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
     if (e != cudaSuccess) return cuda_fail(h, e, "imex_macroscopic");
+    return IMEX_OK;
+}
+
+int imex_velocity_max_diff(imex_lattice* a, imex_lattice* b, double out[2])
+{
+    int rc = check_ready(a, "imex_velocity_max_diff");
+    if (rc) return rc;
+    rc = check_ready(b, "imex_velocity_max_diff");
+    if (rc) return rc;
+    if (!out) return fail(a, IMEX_ERR_ARG, "imex_velocity_max_diff: null output");
+    if (a->g.nx != b->g.nx || a->g.ny != b->g.ny || a->g.nz != b->g.nz || a->device != b->device)
+        return fail(a, IMEX_ERR_ARG, "imex_velocity_max_diff: lattices differ in size or device");
+    IMEX_CUDA(a, cudaStreamSynchronize(b->stream), "imex_velocity_max_diff");
+    const size_t n = a->ncells;
+    double* d = nullptr;
+    IMEX_CUDA(a, cudaMallocAsync(&d, 6 * n * sizeof(double) + 2 * sizeof(unsigned long long), a->stream),
+              "cudaMallocAsync");
+    cudaStream_t keep = b->stream;
+    b->stream = a->stream;  // run b's kernel on a's stream, after a's work
+    rc = macro_fields(a, nullptr, d, d + n, d + 2 * n);
+    if (!rc) rc = macro_fields(b, nullptr, d + 3 * n, d + 4 * n, d + 5 * n);
+    b->stream = keep;
+    unsigned long long* res = reinterpret_cast<unsigned long long*>(d + 6 * n);
+    unsigned long long host[2] = {0, 0};
+    cudaError_t e = rc ? cudaSuccess : launch_maxdiff3(d, d + 3 * n, n, res, a->stream);
+    if (!rc && e == cudaSuccess) {
+        ++a->launches;
+        e = cudaMemcpyAsync(host, res, sizeof host, cudaMemcpyDeviceToHost, a->stream);
+    }
+    cudaError_t e2 = cudaFreeAsync(d, a->stream);
+    if (e == cudaSuccess) e = e2;
+    if (e == cudaSuccess) e = cudaStreamSynchronize(a->stream);
+    if (rc) return rc;
+    if (e != cudaSuccess) return cuda_fail(a, e, "imex_velocity_max_diff");
+    std::memcpy(&out[0], &host[0], 8);
+    std::memcpy(&out[1], &host[1], 8);
     return IMEX_OK;
 }
 
@@ -344,6 +412,19 @@ static int get_f_impl(imex_lattice* h, double* dst, size_t n, cudaMemcpyKind kin
     int rc = check_ready(h, what);
     if (rc) return rc;
     if (!dst || n != (size_t)kQ * h->ncells) return fail(h, IMEX_ERR_ARG, std::string(what) + ": buffer size must be 27*nx*ny*nz");
+    if (lowp(h)) {
+        // convert (pulling through a pending streaming) into a float64 buffer
+        double* tmp = dst;
+        if (kind != cudaMemcpyDeviceToDevice)
+            IMEX_CUDA(h, cudaMallocAsync(&tmp, n * sizeof(double), h->stream), "cudaMallocAsync");
+        cudaError_t e = launch_to_f64(h->precision, h->tag == kPendingStream, h->buf[h->cur], h->g, tmp, h->stream);
+        if (e == cudaSuccess) ++h->launches;
+        if (e == cudaSuccess && tmp != dst) e = cudaMemcpyAsync(dst, tmp, n * sizeof(double), kind, h->stream);
+        if (tmp != dst) cudaFreeAsync(tmp, h->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+        if (e != cudaSuccess) return cuda_fail(h, e, what);
+        return IMEX_OK;
+    }
     rc = materialize(h);
     if (rc) return rc;
     IMEX_CUDA(h, cudaMemcpyAsync(dst, dbuf(h, h->cur), n * sizeof(double), kind, h->stream), what);
@@ -356,8 +437,24 @@ static int set_f_impl(imex_lattice* h, const double* src, size_t n, cudaMemcpyKi
     if (!h) return set_thread_error(IMEX_ERR_ARG, std::string(what) + ": null handle");
     if (!src || n != (size_t)kQ * h->ncells) return fail(h, IMEX_ERR_ARG, std::string(what) + ": buffer size must be 27*nx*ny*nz");
     IMEX_CUDA(h, cudaSetDevice(h->device), "cudaSetDevice");
-    IMEX_CUDA(h, cudaMemcpyAsync(dbuf(h, h->cur), src, n * sizeof(double), kind, h->stream), what);
-    IMEX_CUDA(h, cudaStreamSynchronize(h->stream), what);
+    if (lowp(h)) {
+        const double* dsrc = src;
+        double* tmp = nullptr;
+        cudaError_t e = cudaSuccess;
+        if (kind != cudaMemcpyDeviceToDevice) {
+            e = cudaMallocAsync(&tmp, n * sizeof(double), h->stream);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(tmp, src, n * sizeof(double), kind, h->stream);
+            dsrc = tmp;
+        }
+        if (e == cudaSuccess) e = launch_from_f64(h->precision, dsrc, h->buf[h->cur], h->g, h->stream);
+        if (e == cudaSuccess) ++h->launches;
+        if (tmp) cudaFreeAsync(tmp, h->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+        if (e != cudaSuccess) return cuda_fail(h, e, what);
+    } else {
+        IMEX_CUDA(h, cudaMemcpyAsync(dbuf(h, h->cur), src, n * sizeof(double), kind, h->stream), what);
+        IMEX_CUDA(h, cudaStreamSynchronize(h->stream), what);
+    }
     h->tag = kExact;
     return IMEX_OK;
 }
@@ -378,8 +475,8 @@ int imex_set_engine(imex_lattice* h, int engine)
     if (!h) return set_thread_error(IMEX_ERR_ARG, "imex_set_engine: null handle");
     if (engine != IMEX_ENGINE_AUTO && engine != IMEX_ENGINE_NATIVE && engine != IMEX_ENGINE_FIXED)
         return fail(h, IMEX_ERR_ARG, "imex_set_engine: unknown engine");
-    if (engine == IMEX_ENGINE_FIXED && !h->fx_ok)
-        return fail(h, IMEX_ERR_ARG, "imex_set_engine: fixed-point engine unavailable for these tau/rho0");
+    if (engine == IMEX_ENGINE_FIXED && (!h->fx_ok || lowp(h)))
+        return fail(h, IMEX_ERR_ARG, "imex_set_engine: the fixed-point engine needs float64 storage and 0.75 <= rho0 <= 1.25");
     h->engine = engine;
     return IMEX_OK;
 }

@@ -117,6 +117,12 @@ class LBM:
         self._check(self._L.imex_macroscopic(self._h, *ptr))
         return tuple(arrs)
 
+    def velocity_max_diff(self, ref: "LBM"):
+        """(max |u_self - u_ref|, max |u_ref|) over all cells and components."""
+        out = np.zeros(2)
+        self._check(self._L.imex_velocity_max_diff(self._h, ref._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+        return float(out[0]), float(out[1])
+
     # -- data access --------------------------------------------------------
     def get_f(self, out: np.ndarray | None = None) -> np.ndarray:
         f = np.empty(self.shape) if out is None else out

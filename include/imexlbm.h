@@ -109,6 +109,13 @@ int imex_conserved(imex_lattice *h, double out[5]);
  * (src/lbm.cpp:213-240).  Any output pointer may be NULL. */
 int imex_macroscopic(imex_lattice *h, double *p, double *u, double *v, double *w);
 
+/* Largest velocity difference between two lattices of the same size on
+ * the same GPU: out[0] = max over cells and components of |u_a - u_b|,
+ * out[1] = max |u_b| (u = sum f e per cell, as in src/lbm.cpp:227-235).
+ * Compares a reduced-precision run against a float64 run without moving
+ * the fields to the host.  Synchronises both handles' streams. */
+int imex_velocity_max_diff(imex_lattice *a, imex_lattice *b, double out[2]);
+
 /* Copy the current distributions (reference order, float64) to the host
  * buffer of n = 27*nx*ny*nz values.  The reference exposes them as the
  * public member LBM::f (src/lbm.hpp:165).  Synchronises. */
