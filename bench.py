@@ -245,8 +245,10 @@ def run_ours(a):
             import torch.distributed as dist
             dist.barrier()
 
-    # warm-up (includes the first-step collide-only kernel)
+    # warm-up (includes the first-step collide-only kernel and the launch-shape
+    # autotuner, which times each candidate on this lattice)
     lat.step(max(3, a.warmup))
+    launch_shape = lat.get_launch()
     lat.fence()
     torch.cuda.synchronize()
     barrier()
@@ -339,7 +341,10 @@ def run_ours(a):
                 "dtype": {"fixed": "s64 fixed-point arithmetic, f64 storage", "native": "f64",
                           "float32": "f32 arithmetic, %s storage" % a.precision}[eng_name],
                 "data": "synthetic: Taylor-Green initial field (deterministic, no seed)",
-                "config": workload_config(a, eng_name), "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
+                "config": dict(workload_config(a, eng_name),
+                               launch={"stages": launch_shape[0], "rows_per_stage": launch_shape[1],
+                                       "ctas_per_sm": launch_shape[2], "threads": launch_shape[3]}),
+                "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
                 "gpu_launches": gpu_launches, "clocks": clk.summary(),
                 "fallback_cells": fallback, "mass": cons[0], "ke": cons[4],
                 "roofline_glups_at_peak": round(hbm / bpc, 3)}

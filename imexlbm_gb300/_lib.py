@@ -63,6 +63,8 @@ SIGNATURES = {
     "imex_set_f_device": (ctypes.c_int, [_h, ctypes.c_void_p, ctypes.c_size_t]),
     "imex_conserved_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                               ctypes.c_void_p, ctypes.c_void_p]),
+    "imex_set_launch": (ctypes.c_int, [_h, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    "imex_get_launch": (ctypes.c_int, [_h, ctypes.POINTER(ctypes.c_int)]),
     "imex_set_engine": (ctypes.c_int, [_h, ctypes.c_int]),
     "imex_set_stream": (ctypes.c_int, [_h, ctypes.c_void_p]),
     "imex_synchronize": (ctypes.c_int, [_h]),

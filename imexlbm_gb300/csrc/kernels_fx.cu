@@ -19,6 +19,7 @@
 #include "collide_f64.cuh"
 #include "fx_math.cuh"
 #include "kernels_fx.cuh"
+#include "rows.cuh"
 
 namespace imex {
 
@@ -67,7 +68,61 @@ __global__ void __launch_bounds__(kStepBlock) k_step_fx(const double* __restrict
     if (!ok) fallback_cell(src, dst, g, i, j, k, cp, fallback);
 }
 
+// Native float64 redo of one cell of a staged row.
+__device__ __noinline__ void fallback_staged(const double* __restrict__ st, int astride, int nz, int z, CollideF64 cp,
+                                             double* __restrict__ dst, size_t plane, size_t rowoff,
+                                             unsigned long long* fallback)
+{
+    const int zm = z == 0 ? nz - 1 : z - 1, zp = z == nz - 1 ? 0 : z + 1;
+    double h[kQ];
+#pragma unroll
+    for (int a = 0; a < kQ; ++a) h[a] = st[a * astride + pull_z(ex(a, 2), z, zm, zp)];
+    collide_f64(h, cp);
+#pragma unroll
+    for (int a = 0; a < kQ; ++a) dst[(size_t)a * plane + rowoff + z] = h[a];
+    atomicAdd(fallback, 1ull);
+}
+
+// Row-kernel engine: fixed-point collision of one staged cell.
+template <bool OM_GE1, int MINB>
+struct EngFx {
+    using T = double;
+    static constexpr int kMinBlocks = MINB;
+    FxConst c;
+    CollideF64 cp;
+    unsigned long long* fallback;
+
+    __device__ __forceinline__ void run(const double* __restrict__ st, int astride, int nz, int z,
+                                        double* __restrict__ dst, size_t plane, size_t rowoff) const
+    {
+        const int zm = z == 0 ? nz - 1 : z - 1, zp = z == nz - 1 ? 0 : z + 1;
+        double f[kQ];
+#pragma unroll
+        for (int a = 0; a < kQ; ++a) f[a] = st[a * astride + pull_z(ex(a, 2), z, zm, zp)];
+        bool ok = true;
+        double out[kQ];
+        fx::collide_cell<OM_GE1>(f, out, c, ok);
+#pragma unroll
+        for (int a = 0; a < kQ; ++a) dst[(size_t)a * plane + rowoff + z] = out[a];
+        if (!ok) fallback_staged(st, astride, nz, z, cp, dst, plane, rowoff, fallback);
+    }
+};
+
 }  // namespace
+
+bool rows_fx_eligible(const Geom& g) { return rows_eligible<double>(g); }
+
+cudaError_t launch_rows_fx(const double* src, double* dst, const Geom& g, const FxParams& fx, const CollideF64& cp,
+                           unsigned long long* fallback, const RowConfig& rc, unsigned* err, cudaStream_t s)
+{
+    // One resident CTA per SM lets the compiler keep the whole cell in
+    // registers; two cap it at 128 registers per thread.
+    if (rc.ctas_per_sm <= 1)
+        return fx.om_ge1 ? launch_rows(src, dst, g, EngFx<true, 1>{fx.k, cp, fallback}, rc, err, s)
+                         : launch_rows(src, dst, g, EngFx<false, 1>{fx.k, cp, fallback}, rc, err, s);
+    return fx.om_ge1 ? launch_rows(src, dst, g, EngFx<true, 2>{fx.k, cp, fallback}, rc, err, s)
+                     : launch_rows(src, dst, g, EngFx<false, 2>{fx.k, cp, fallback}, rc, err, s);
+}
 
 cudaError_t launch_step_fx(int mode, const double* src, double* dst, const Geom& g, const FxParams& fx,
                            const CollideF64& cp, unsigned long long* fallback, cudaStream_t s)

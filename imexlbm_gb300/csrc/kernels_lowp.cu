@@ -31,6 +31,7 @@
 #include <cuda_fp16.h>
 
 #include "kernels_lowp.cuh"
+#include "rows.cuh"
 #include "tg_init.cuh"
 
 namespace imex {
@@ -140,6 +141,26 @@ __global__ void __launch_bounds__(kStepBlock) k_step_lowp(const typename Storage
 #pragma unroll
     for (int a = 0; a < kQ; ++a) dst[(size_t)a * g.plane + cell] = S::store(h[a], a);
 }
+
+// Row-kernel engine: float32 collision of one staged cell.
+template <int P>
+struct EngLowp {
+    using T = typename Storage<P>::T;
+    static constexpr int kMinBlocks = 4;
+    CollideF32 cp;
+
+    __device__ __forceinline__ void run(const T* __restrict__ st, int astride, int nz, int z, T* __restrict__ dst,
+                                        size_t plane, size_t rowoff) const
+    {
+        const int zm = z == 0 ? nz - 1 : z - 1, zp = z == nz - 1 ? 0 : z + 1;
+        float h[kQ];
+#pragma unroll
+        for (int a = 0; a < kQ; ++a) h[a] = Storage<P>::load_plain(st + a * astride + pull_z(ex(a, 2), z, zm, zp), a);
+        collide_dev_f32(h, cp);
+#pragma unroll
+        for (int a = 0; a < kQ; ++a) dst[(size_t)a * plane + rowoff + z] = Storage<P>::store(h[a], a);
+    }
+};
 
 // Taylor-Green initial state (float64 equilibrium, src/lbm.cpp:78-108),
 // rounded once into the storage format.
@@ -302,6 +323,22 @@ cudaError_t launch_step_lowp(int prec, int mode, const void* src, void* dst, con
     return prec == IMEX_F32 ? step_impl<IMEX_F32>(mode, src, dst, g, cp, s)
                             : step_impl<IMEX_F16DEV>(mode, src, dst, g, cp, s);
 }
+
+bool rows_lowp_eligible(int prec, const Geom& g)
+{
+    return prec == IMEX_F32 ? rows_eligible<float>(g) : rows_eligible<__half>(g);
+}
+
+cudaError_t launch_rows_lowp(int prec, const void* src, void* dst, const Geom& g, const CollideF32& cp,
+                             const RowConfig& rc, unsigned* err, cudaStream_t s)
+{
+    if (prec == IMEX_F32)
+        return launch_rows(static_cast<const float*>(src), static_cast<float*>(dst), g, EngLowp<IMEX_F32>{cp}, rc, err, s);
+    return launch_rows(static_cast<const __half*>(src), static_cast<__half*>(dst), g, EngLowp<IMEX_F16DEV>{cp}, rc,
+                       err, s);
+}
+
+size_t rows_lowp_stage_bytes(int prec, int nz) { return (size_t)kQ * nz * (prec == IMEX_F32 ? 4 : 2); }
 
 cudaError_t launch_from_f64(int prec, const double* f, void* out, const Geom& g, cudaStream_t s)
 {

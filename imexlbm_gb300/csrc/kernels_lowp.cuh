@@ -18,6 +18,11 @@ struct CollideF32 {
 
 CollideF32 make_collide_f32(double tau0);
 
+struct RowConfig;
+bool rows_lowp_eligible(int prec, const Geom& g);
+size_t rows_lowp_stage_bytes(int prec, int nz);
+cudaError_t launch_rows_lowp(int prec, const void* src, void* dst, const Geom& g, const CollideF32& cp,
+                             const RowConfig& rc, unsigned* err, cudaStream_t s);
 cudaError_t launch_init_lowp(int prec, void* f, const Geom& g, const double* tx, const double* ty, const double* tz,
                              double rho0, double u0, cudaStream_t s);
 cudaError_t launch_step_lowp(int prec, int mode, const void* src, void* dst, const Geom& g, const CollideF32& cp,

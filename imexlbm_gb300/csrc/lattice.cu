@@ -18,14 +18,19 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <new>
 #include <string>
+#include <tuple>
+#include <vector>
 
 #include "imexlbm.h"
 #include "imexlbm_internal.hpp"
 #include "kernels_f64.cuh"
 #include "kernels_fx.cuh"
 #include "kernels_lowp.cuh"
+#include "rows.cuh"
 
 namespace imex {
 
@@ -68,6 +73,9 @@ struct imex_lattice {
     CollideF32 cf32{};
     FxParams fx{};
     bool fx_ok = false;  // fixed-point engine usable for this lattice
+    unsigned* d_err = nullptr;  // set by kernels whose bounded waits ran out
+    RowConfig rows{};           // launch shape of the fused step (stages 0: one thread per cell)
+    int shape_mode = -1;        // -1 autotune on first use, 0 one thread per cell, 1 row-staged
     std::string err;
 };
 
@@ -104,6 +112,155 @@ double* dbuf(imex_lattice* h, int which) { return static_cast<double*>(h->buf[wh
 
 bool lowp(const imex_lattice* h) { return h->precision != IMEX_F64; }
 
+// ------------------------------------------------------------ launch shapes --
+// The fused step has two kernels: one thread per cell with direct pulls
+// from global memory, and the row-staged kernel (rows.cuh) whose shape is a
+// ring depth and a number of resident CTAs per SM.  The autotuner times each
+// candidate shape on the handle's own lattice - the fused kernel reads one
+// buffer and writes the other, so repeating it changes nothing - and keeps
+// the fastest.  Results are cached per (precision, engine, nx, ny, nz).
+
+bool rows_eligible_for(const imex_lattice* h)
+{
+    if (lowp(h)) return rows_lowp_eligible(h->precision, h->g);
+    return use_fixed(h) && rows_fx_eligible(h->g);
+}
+
+size_t stage_bytes(const imex_lattice* h) { return (size_t)kQ * h->g.nz * elem_size(h->precision); }
+
+std::vector<RowConfig> row_candidates(const imex_lattice* h)
+{
+    std::vector<RowConfig> out;
+    if (!rows_eligible_for(h)) return out;
+    const size_t sb = stage_bytes(h);  // one row of all 27 directions
+    const size_t per_sm = 227 * 1024;
+    const int threads = h->g.nz >= 256 ? 256 : ((h->g.nz + 31) / 32) * 32;
+    const int ctas_opts[3] = {1, 2, 4};
+    const int stage_opts[3] = {2, 3, 4};
+    const int rows_opts[4] = {1, 2, 4, 8};
+    for (int c : ctas_opts) {
+        if (!lowp(h) && c > 2) continue;  // fixed-point engine: 128+ registers per thread
+        for (int B : rows_opts) {
+            if (h->g.ny % B) continue;
+            for (int s : stage_opts) {
+                const size_t smem = kRowBarrierBytes + (size_t)s * B * sb;
+                if (smem > per_sm / c) continue;
+                if ((size_t)s * B * sb < 24 * 1024) continue;  // too little in flight to matter
+                RowConfig rc;
+                rc.stages = s;
+                rc.rows = B;
+                rc.ctas_per_sm = c;
+                rc.threads = threads;
+                out.push_back(rc);
+            }
+        }
+    }
+    return out;
+}
+
+std::mutex g_tune_lock;
+std::map<std::tuple<int, int, int, int, int>, RowConfig> g_tune_cache;
+
+std::tuple<int, int, int, int, int> tune_key(const imex_lattice* h)
+{
+    return std::make_tuple(h->precision, use_fixed(h) ? 1 : 0, h->g.nx, h->g.ny, h->g.nz);
+}
+
+cudaError_t launch_fused_rows(imex_lattice* h, const void* src, void* dst, const RowConfig& rc)
+{
+    if (lowp(h)) return launch_rows_lowp(h->precision, src, dst, h->g, h->cf32, rc, h->d_err, h->stream);
+    return launch_rows_fx(static_cast<const double*>(src), static_cast<double*>(dst), h->g, h->fx, h->cf64,
+                          h->d_fallback, rc, h->d_err, h->stream);
+}
+
+cudaError_t launch_fused_classic(imex_lattice* h, const void* src, void* dst)
+{
+    if (lowp(h)) return launch_step_lowp(h->precision, kModeFused, src, dst, h->g, h->cf32, h->stream);
+    if (use_fixed(h))
+        return launch_step_fx(kModeFused, static_cast<const double*>(src), static_cast<double*>(dst), h->g, h->fx,
+                              h->cf64, h->d_fallback, h->stream);
+    return launch_step_f64(kModeFused, static_cast<const double*>(src), static_cast<double*>(dst), h->g, h->cf64,
+                           h->stream);
+}
+
+// Time the fused step in shape rc (stages 0: classic); milliseconds per launch.
+int time_shape(imex_lattice* h, const RowConfig& rc, float* ms)
+{
+    const void* src = h->buf[h->cur];
+    void* dst = h->buf[1 - h->cur];
+    cudaEvent_t e0, e1;
+    IMEX_CUDA(h, cudaEventCreate(&e0), "cudaEventCreate");
+    IMEX_CUDA(h, cudaEventCreate(&e1), "cudaEventCreate");
+    cudaError_t e = cudaSuccess;
+    const int reps = 3;
+    for (int r = 0; r <= reps && e == cudaSuccess; ++r) {
+        if (r == 1) e = cudaEventRecord(e0, h->stream);
+        if (e == cudaSuccess) e = rc.stages > 0 ? launch_fused_rows(h, src, dst, rc) : launch_fused_classic(h, src, dst);
+        if (e == cudaSuccess) h->launches++;
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(e1, h->stream);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (e != cudaSuccess) return cuda_fail(h, e, "autotune");
+    *ms /= reps;
+    return IMEX_OK;
+}
+
+int tune(imex_lattice* h)
+{
+    std::vector<RowConfig> cands = row_candidates(h);
+    RowConfig best{};  // classic
+    if (!cands.empty()) {
+        float best_ms = 0.f;
+        int rc = time_shape(h, best, &best_ms);
+        if (rc) return rc;
+        for (const RowConfig& c : cands) {
+            float ms = 0.f;
+            rc = time_shape(h, c, &ms);
+            if (rc) return rc;
+            if (ms < best_ms) {
+                best_ms = ms;
+                best = c;
+            }
+        }
+    }
+    h->rows = best;
+    std::lock_guard<std::mutex> guard(g_tune_lock);
+    g_tune_cache[tune_key(h)] = best;
+    return IMEX_OK;
+}
+
+// Pick the fused step's launch shape before its first use: a pinned shape,
+// a cached result, the tuner, or - while the stream is being captured into
+// a graph, where the tuner cannot synchronise - the first candidate.
+int ensure_tuned(imex_lattice* h)
+{
+    if (h->shape_mode >= 0) return IMEX_OK;
+    {
+        std::lock_guard<std::mutex> guard(g_tune_lock);
+        auto it = g_tune_cache.find(tune_key(h));
+        if (it != g_tune_cache.end()) {
+            h->rows = it->second;
+            h->shape_mode = h->rows.stages > 0 ? 1 : 0;
+            return IMEX_OK;
+        }
+    }
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    IMEX_CUDA(h, cudaStreamIsCapturing(h->stream, &cs), "cudaStreamIsCapturing");
+    if (cs != cudaStreamCaptureStatusNone) {
+        std::vector<RowConfig> c = row_candidates(h);
+        h->rows = c.empty() ? RowConfig{} : c.front();
+        h->shape_mode = h->rows.stages > 0 ? 1 : 0;
+        return IMEX_OK;
+    }
+    int rc = tune(h);
+    if (rc) return rc;
+    h->shape_mode = h->rows.stages > 0 ? 1 : 0;
+    return IMEX_OK;
+}
+
 // One step-kernel launch in `mode` from buf[cur] into buf[cur] (collide) or
 // buf[1 - cur] (fused / stream).
 int launch_mode(imex_lattice* h, int mode)
@@ -111,7 +268,13 @@ int launch_mode(imex_lattice* h, int mode)
     const double* src = dbuf(h, h->cur);
     double* dst = mode == kModeCollide ? dbuf(h, h->cur) : dbuf(h, 1 - h->cur);
     cudaError_t e;
-    if (lowp(h))
+    if (mode == kModeFused) {
+        int rc = ensure_tuned(h);
+        if (rc) return rc;
+    }
+    if (mode == kModeFused && h->rows.stages > 0)
+        e = launch_fused_rows(h, src, dst, h->rows);
+    else if (lowp(h))
         e = launch_step_lowp(h->precision, mode, src, dst, h->g, h->cf32, h->stream);
     else if (mode != kModeStream && use_fixed(h))
         e = launch_step_fx(mode, src, dst, h->g, h->fx, h->cf64, h->d_fallback, h->stream);
@@ -133,6 +296,19 @@ int check_ready(imex_lattice* h, const char* what)
 
 // Make the device buffer hold the reference's f exactly (apply a pending
 // streaming into the other buffer).
+// A kernel's bounded wait ran out (see bulk.cuh): report it once.
+int check_kernel_error(imex_lattice* h)
+{
+    unsigned v = 0;
+    IMEX_CUDA(h, cudaMemcpyAsync(&v, h->d_err, sizeof v, cudaMemcpyDeviceToHost, h->stream), "cudaMemcpy");
+    IMEX_CUDA(h, cudaStreamSynchronize(h->stream), "kernel status");
+    if (v) {
+        IMEX_CUDA(h, cudaMemsetAsync(h->d_err, 0, sizeof v, h->stream), "cudaMemset");
+        return fail(h, IMEX_ERR_CUDA, "a kernel's asynchronous copy did not complete in time; its results are invalid");
+    }
+    return IMEX_OK;
+}
+
 int materialize(imex_lattice* h)
 {
     if (h->tag != kPendingStream) return IMEX_OK;
@@ -203,12 +379,14 @@ int imex_create(int nx, int ny, int nz, double tau, double rho0, double u0, int 
     e = cudaMalloc(&h->d_partial, nparts * 5 * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&h->d_out, 5 * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&h->d_fallback, sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMalloc(&h->d_err, sizeof(unsigned));
     if (e == cudaSuccess) e = cudaMallocHost(&h->h_out, 5 * sizeof(double));
     if (e != cudaSuccess) return bail(set_thread_error(IMEX_ERR_MEMORY, "imex_create: scratch allocation failed"));
     e = cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) return bail(cuda_fail(nullptr, e, "cudaStreamCreate"));
     h->stream = h->own_stream;
     e = cudaMemsetAsync(h->d_fallback, 0, sizeof(unsigned long long), h->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(h->d_err, 0, sizeof(unsigned), h->stream);
     if (e != cudaSuccess) return bail(cuda_fail(nullptr, e, "cudaMemset"));
     h->bytes = 2 * arr + nparts * 5 * sizeof(double) + 5 * sizeof(double) + sizeof(unsigned long long);
     *out = h;
@@ -225,6 +403,7 @@ void imex_destroy(imex_lattice* h)
     if (h->d_partial) cudaFree(h->d_partial);
     if (h->d_out) cudaFree(h->d_out);
     if (h->d_fallback) cudaFree(h->d_fallback);
+    if (h->d_err) cudaFree(h->d_err);
     if (h->h_out) cudaFreeHost(h->h_out);
     if (h->own_stream) cudaStreamDestroy(h->own_stream);
     delete h;
@@ -322,6 +501,8 @@ int imex_conserved(imex_lattice* h, double out[5])
     h->launches += 2;
     IMEX_CUDA(h, cudaMemcpyAsync(h->h_out, h->d_out, 5 * sizeof(double), cudaMemcpyDeviceToHost, h->stream), "cudaMemcpy");
     IMEX_CUDA(h, cudaStreamSynchronize(h->stream), "imex_conserved");
+    rc = check_kernel_error(h);
+    if (rc) return rc;
     bool finite = true;
     for (int q = 0; q < 5; ++q) {
         out[q] = h->h_out[q];
@@ -492,6 +673,47 @@ int imex_synchronize(imex_lattice* h)
 {
     if (!h) return set_thread_error(IMEX_ERR_ARG, "imex_synchronize: null handle");
     IMEX_CUDA(h, cudaStreamSynchronize(h->stream), "imex_synchronize");
+    return check_kernel_error(h);
+}
+
+int imex_set_launch(imex_lattice* h, int stages, int rows_per_stage, int ctas_per_sm)
+{
+    if (!h) return set_thread_error(IMEX_ERR_ARG, "imex_set_launch: null handle");
+    if (stages < 0) {
+        h->shape_mode = -1;
+        return IMEX_OK;
+    }
+    if (stages == 0) {
+        h->rows = RowConfig{};
+        h->shape_mode = 0;
+        return IMEX_OK;
+    }
+    if (!rows_eligible_for(h))
+        return fail(h, IMEX_ERR_ARG, "imex_set_launch: the row-staged kernel needs nz*element size a multiple of 16 "
+                                     "bytes and a fixed-point or reduced-precision engine");
+    const int B = rows_per_stage < 1 ? 1 : rows_per_stage;
+    if (h->g.ny % B) return fail(h, IMEX_ERR_ARG, "imex_set_launch: rows_per_stage must divide ny");
+    if (stages < 2 || stages > 16 || kRowBarrierBytes + (size_t)stages * B * stage_bytes(h) > 227 * 1024)
+        return fail(h, IMEX_ERR_ARG, "imex_set_launch: ring does not fit in shared memory (2 <= stages <= 16)");
+    RowConfig rc;
+    rc.stages = stages;
+    rc.rows = B;
+    rc.ctas_per_sm = ctas_per_sm < 1 ? 1 : ctas_per_sm;
+    rc.threads = h->g.nz >= 256 ? 256 : ((h->g.nz + 31) / 32) * 32;
+    h->rows = rc;
+    h->shape_mode = 1;
+    return IMEX_OK;
+}
+
+int imex_get_launch(imex_lattice* h, int out[4])
+{
+    if (!h || !out) return set_thread_error(IMEX_ERR_ARG, "imex_get_launch: null argument");
+    int rc = ensure_tuned(h);
+    if (rc) return rc;
+    out[0] = h->rows.stages;
+    out[1] = h->rows.stages ? h->rows.rows : 0;
+    out[2] = h->rows.ctas_per_sm;
+    out[3] = h->rows.threads;
     return IMEX_OK;
 }
 

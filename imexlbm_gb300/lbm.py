@@ -144,6 +144,19 @@ class LBM:
     def set_engine(self, engine: int) -> None:
         self._check(self._L.imex_set_engine(self._h, int(engine)))
 
+    def set_launch(self, stages: int, rows_per_stage: int = 1, ctas_per_sm: int = 1) -> None:
+        """Pin the fused step's launch shape (stages 0: one thread per cell;
+        >= 2: row-staged ring depth, with rows_per_stage y-rows per item and
+        ctas_per_sm resident CTAs; < 0: automatic)."""
+        self._check(self._L.imex_set_launch(self._h, int(stages), int(rows_per_stage), int(ctas_per_sm)))
+
+    def get_launch(self):
+        """(stages, rows_per_stage, ctas_per_sm, threads) of the fused step,
+        tuning first if needed."""
+        out = (ctypes.c_int * 4)()
+        self._check(self._L.imex_get_launch(self._h, out))
+        return tuple(out)
+
     def set_stream(self, stream_ptr: int | None) -> None:
         self._check(self._L.imex_set_stream(self._h, ctypes.c_void_p(stream_ptr or 0)))
 

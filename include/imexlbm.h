@@ -150,6 +150,25 @@ int imex_set_f_device(imex_lattice *h, const double *dev, size_t n);
  * Errors are reported through imex_last_error(NULL). */
 int imex_conserved_noalloc(const double *f_dev, int nx, int ny, int nz, double *out_dev, void *stream);
 
+/* Launch shape of the fused step.  stages = 0: one thread per cell pulling
+ * straight from global memory.  stages >= 2: the row-staged kernel - each
+ * CTA keeps a ring of `stages` work items in shared memory, an item being
+ * rows_per_stage consecutive y-rows (dividing ny) whose 27 source row runs
+ * arrive by asynchronous bulk copies - with ctas_per_sm resident CTAs per
+ * SM; it needs nz * element size a multiple of 16 bytes and the fixed-point
+ * or a reduced-precision engine.  stages < 0: back to automatic.  By
+ * default the first fused step of a handle times every eligible shape on
+ * the handle's own lattice (without changing its state) and keeps the
+ * fastest, cached per lattice shape for the process; while the handle's
+ * stream is being captured into a CUDA graph it takes the first eligible
+ * shape instead.  No counterpart in the reference (Kokkos picks its own
+ * tiles, src/lbm.cpp:135-139). */
+int imex_set_launch(imex_lattice *h, int stages, int rows_per_stage, int ctas_per_sm);
+
+/* The shape in use: out = {stages, rows_per_stage, ctas_per_sm, threads per
+ * CTA}; runs the autotuner first if no shape has been chosen yet. */
+int imex_get_launch(imex_lattice *h, int out[4]);
+
 /* Select the float64 arithmetic engine (IMEX_ENGINE_*).  Default AUTO. */
 int imex_set_engine(imex_lattice *h, int engine);
 
