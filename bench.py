@@ -53,6 +53,8 @@ def parse_args(argv=None):
     ap.add_argument("--engine", choices=["auto", "native", "fixed"], default="auto")
     ap.add_argument("--precision", choices=["f64", "f32", "f16dev"], default="f64",
                     help="storage precision (f64: the reference's; f32 / f16dev: the reduced-precision variants)")
+    ap.add_argument("--rounding", choices=["nearest", "stochastic"], default="nearest",
+                    help="float16-deviation storage rounding")
     ap.add_argument("--size", type=int, default=256, help="cubic lattice edge (default: the shipped deck's 256)")
     ap.add_argument("--report-every", type=int, default=100)
     ap.add_argument("--no-e2e", action="store_true")
@@ -204,6 +206,8 @@ def workload_config(a, engine):
     desc = {"f64": "float64 distributions", "f32": "float32 distributions",
             "f16dev": "float16 deviations f - w"}[prec]
     esize = {"f64": 8, "f32": 4, "f16dev": 2}[prec]
+    if prec == "f16dev":
+        desc += ", %s rounding" % getattr(a, "rounding", "nearest")
     return {"workload": f"taylor-green {a.size}^3 periodic D3Q27, Re=1600, u0=0.05, {desc}",
             "grid": [a.size] * 3, "precision": prec, "engine": engine, "report_every": a.report_every,
             "l2": "inputs larger than L2 (2 arrays x %.2f GB), no flush" % (27 * a.size ** 3 * esize / 1e9),
@@ -233,6 +237,8 @@ def run_ours(a):
     stream = torch.cuda.Stream()
     lat = m.LBM(n, n, n, d["tau"], d["rho0"], d["u0"], precision=prec, engine=engine)
     lat.set_stream(stream.cuda_stream)
+    if a.precision == "f16dev":
+        lat.set_rounding(m.IMEX_ROUND_STOCHASTIC if a.rounding == "stochastic" else m.IMEX_ROUND_NEAREST)
     lat.Initialize()
     eng_name = "fixed" if (engine == m.IMEX_ENGINE_FIXED) else "native" if engine == m.IMEX_ENGINE_NATIVE else "auto"
     if prec != m.IMEX_F64:
@@ -294,6 +300,8 @@ def run_ours(a):
         host = torch.empty(nval, dtype=torch.float64, pin_memory=True)
         lat2 = m.LBM(n, n, n, d["tau"], d["rho0"], d["u0"], precision=prec, engine=engine)
         lat2.set_stream(stream.cuda_stream)
+        if a.precision == "f16dev":
+            lat2.set_rounding(m.IMEX_ROUND_STOCHASTIC if a.rounding == "stochastic" else m.IMEX_ROUND_NEAREST)
         lat2.Initialize()
         import ctypes
         L = m.load()

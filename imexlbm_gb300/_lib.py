@@ -23,6 +23,9 @@ IMEX_F64 = 0
 IMEX_F32 = 1
 IMEX_F16DEV = 2
 
+IMEX_ROUND_NEAREST = 0
+IMEX_ROUND_STOCHASTIC = 1
+
 IMEX_ENGINE_AUTO = 0
 IMEX_ENGINE_NATIVE = 1
 IMEX_ENGINE_FIXED = 2
@@ -66,6 +69,7 @@ SIGNATURES = {
     "imex_set_launch": (ctypes.c_int, [_h, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     "imex_get_launch": (ctypes.c_int, [_h, ctypes.POINTER(ctypes.c_int)]),
     "imex_set_engine": (ctypes.c_int, [_h, ctypes.c_int]),
+    "imex_set_rounding": (ctypes.c_int, [_h, ctypes.c_int]),
     "imex_set_stream": (ctypes.c_int, [_h, ctypes.c_void_p]),
     "imex_synchronize": (ctypes.c_int, [_h]),
     "imex_steps_done": (ctypes.c_int64, [_h]),
@@ -74,6 +78,19 @@ SIGNATURES = {
     "imex_device_bytes": (ctypes.c_size_t, [_h]),
     "imex_last_error": (ctypes.c_char_p, [_h]),
     "imex_version": (ctypes.c_char_p, []),
+    "imex_initialize_phase": (ctypes.c_int, [_h, ctypes.c_double, ctypes.c_double, ctypes.c_double]),
+    "imex_batch_create": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]),
+    "imex_batch_destroy": (None, [ctypes.c_void_p]),
+    "imex_batch_add": (ctypes.c_int, [ctypes.c_void_p, _h, ctypes.c_int64]),
+    "imex_batch_remove": (ctypes.c_int, [ctypes.c_void_p, _h]),
+    "imex_batch_size": (ctypes.c_int, [ctypes.c_void_p]),
+    "imex_batch_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "imex_batch_synchronize": (ctypes.c_int, [ctypes.c_void_p]),
+    "imex_batch_set_launch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    "imex_batch_get_launch": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]),
+    "imex_batch_set_graph": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "imex_batch_kernel_launches": (ctypes.c_int64, [ctypes.c_void_p]),
+    "imex_batch_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
 }
 
 _lib = None

@@ -1,0 +1,516 @@
+// Batched step: many reduced-precision lattices of any sizes advance in one
+// persistent launch over a packed cell index.
+//
+// A batch holds member lattice handles (float32 or float16-deviation
+// storage).  Their cells are numbered consecutively - lattice after
+// lattice, each in its own f[a][x][y][z] order - and every launch of the
+// persistent kernel walks that packed index: a thread finds its lattice by
+// binary search over the members' first-cell indices, decodes (x, y, z),
+// pulls the 27 values from that lattice's buffer with periodic wrap,
+// collides in float32 (lowp_math.cuh, the same arithmetic as the
+// one-lattice kernels, so results are bit-identical) and writes the other
+// buffer.  Lattices of different sizes, viscosities and storage formats mix
+// in one launch; no launch is spent on a small lattice alone.
+//
+// The member table lives in device memory and the kernel reads it at every
+// launch, so a CUDA graph of K launches (step index s = 0..K-1 baked in)
+// stays valid while members join, leave or finish: a member runs at step s
+// only while s < its step count for the tick, and within a tick it reads
+// buf[cur ^ (s & 1)] and writes the other buffer.
+//
+// Launch shape (threads per CTA, cells per thread, CTAs per SM) is chosen
+// by an autotuner that times each candidate on the batch itself; timing
+// writes only the members' spare buffers, so it changes no state.
+#include <algorithm>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "imexlbm.h"
+#include "imexlbm_internal.hpp"
+#include "lattice_internal.hpp"
+#include "lowp_math.cuh"
+
+namespace imex {
+
+namespace {
+
+constexpr int kBatchMax = 2048;  // members per batch (shared-memory search table)
+
+struct BatchEntry {
+    unsigned long long begin;  // packed index of the member's first cell
+    unsigned long long plane;  // cells of the member
+    void* buf[2];
+    int nx, ny, nz;
+    int prec;   // IMEX_F32 or IMEX_F16DEV
+    int cur;    // buffer holding the member's state at the start of the tick
+    int steps;  // fused steps this tick
+    float eps;      // 2 - omega
+    int sr;         // float16 storage: stochastic rounding
+    uint32_t seed;  // stochastic-rounding seed at the start of the tick
+    int pad;
+};
+
+struct BatchHeader {
+    unsigned long long total;  // cells of all members
+    int count;
+    int pad;
+};
+
+template <int P>
+__device__ __forceinline__ void batch_cell(const BatchEntry& e, unsigned long long local, int s, const CollideF32& base)
+{
+    using S = lowp::Storage<P>;
+    using T = typename S::T;
+    const int nz = e.nz, ny = e.ny, nx = e.nx;
+    const unsigned l32 = (unsigned)local;  // members hold fewer than 2^32 cells
+    const unsigned row = l32 / (unsigned)nz;
+    const int k = (int)(l32 - row * (unsigned)nz);
+    const int i = (int)(row / (unsigned)ny);
+    const int j = (int)(row - (unsigned)i * (unsigned)ny);
+    Geom g;
+    g.nx = nx;
+    g.ny = ny;
+    g.nz = nz;
+    g.plane = e.plane;
+    const PullIndex pi(g, i, j, k, true);
+    const T* src = static_cast<const T*>(e.buf[e.cur ^ (s & 1)]);
+    T* dst = static_cast<T*>(e.buf[e.cur ^ (s & 1) ^ 1]);
+    float h[kQ];
+#pragma unroll
+    for (int a = 0; a < kQ; ++a) h[a] = S::load(src + pi.at_dyn(g, a), a);
+    CollideF32 cp = base;
+    cp.eps = e.eps;
+    lowp::collide_dev_f32(h, cp);
+    if constexpr (P == IMEX_F16DEV) {
+        if (e.sr) {
+            const uint32_t ch = lowp::sr_hash(local, e.seed + (uint32_t)s);
+#pragma unroll
+            for (int a = 0; a < kQ; ++a) h[a] = S::round_sr(h[a], lowp::sr_bits(ch, a));
+        }
+        lowp::store_f16_cell(h, [&](int a) -> T& { return dst[(size_t)a * e.plane + local]; });
+        return;
+    }
+#pragma unroll
+    for (int a = 0; a < kQ; ++a) dst[(size_t)a * e.plane + local] = S::store(h[a], a);
+}
+
+// CPT cells per thread, strided by blockDim within a chunk of CPT*blockDim.
+template <int CPT>
+__global__ void __launch_bounds__(256) k_batch(const BatchHeader* __restrict__ hdr, const BatchEntry* __restrict__ tab, int s,
+                                               CollideF32 base)
+{
+    __shared__ unsigned long long sbegin[kBatchMax + 1];
+    const int count = hdr->count;
+    const unsigned long long total = hdr->total;
+    for (int q = threadIdx.x; q < count; q += blockDim.x) sbegin[q] = tab[q].begin;
+    if (threadIdx.x == 0) sbegin[count] = total;
+    __syncthreads();
+    const unsigned long long chunk = (unsigned long long)blockDim.x * CPT;
+    for (unsigned long long c0 = (unsigned long long)blockIdx.x * chunk; c0 < total; c0 += (unsigned long long)gridDim.x * chunk) {
+#pragma unroll
+        for (int c = 0; c < CPT; ++c) {
+            const unsigned long long q = c0 + (unsigned long long)c * blockDim.x + threadIdx.x;
+            if (q >= total) break;
+            int lo = 0, hi = count;  // largest lo with sbegin[lo] <= q
+            while (hi - lo > 1) {
+                const int mid = (lo + hi) >> 1;
+                if (sbegin[mid] <= q) lo = mid;
+                else hi = mid;
+            }
+            const BatchEntry& e = tab[lo];
+            if (s >= e.steps) continue;
+            if (e.prec == IMEX_F32) batch_cell<IMEX_F32>(e, q - sbegin[lo], s, base);
+            else batch_cell<IMEX_F16DEV>(e, q - sbegin[lo], s, base);
+        }
+    }
+}
+
+}  // namespace
+
+}  // namespace imex
+
+using namespace imex;
+
+struct BatchShape {
+    int threads = 0, cpt = 0, ctas_per_sm = 0;  // 0: not chosen yet
+};
+
+struct imex_batch {
+    std::vector<imex_lattice*> members;
+    std::vector<int64_t> limit;  // total reference steps after which a member stops (-1: none)
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr;
+    BatchHeader* d_hdr = nullptr;
+    BatchEntry* d_tab = nullptr;
+    BatchHeader* h_hdr = nullptr;  // pinned staging
+    BatchEntry* h_tab = nullptr;
+    int capacity = 0;
+    int device = 0;
+    int sms = 0;
+    BatchShape shape;
+    bool shape_pinned = false;
+    int graph_steps = 0;  // K of the captured graph (0: no graph)
+    cudaGraphExec_t graph = nullptr;
+    int graph_k = 0;
+    BatchShape graph_shape;
+    int64_t launches = 0;
+    std::string err;
+};
+
+namespace {
+
+int bfail(imex_batch* b, int code, const std::string& msg)
+{
+    if (b) b->err = msg;
+    return set_thread_error(code, msg);
+}
+
+int bcuda(imex_batch* b, cudaError_t e, const char* what)
+{
+    cudaGetLastError();
+    return bfail(b, IMEX_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define B_CUDA(b, call, what)                            \
+    do {                                                 \
+        cudaError_t e_ = (call);                         \
+        if (e_ != cudaSuccess) return bcuda(b, e_, what); \
+    } while (0)
+
+CollideF32 base_constants()
+{
+    // eps is per member; w and the e.u coefficients are shared.
+    return make_collide_f32(0.0);
+}
+
+cudaError_t launch_batch(imex_batch* b, const BatchShape& sh, int s)
+{
+    const CollideF32 base = base_constants();
+    const dim3 grid((unsigned)(b->sms * sh.ctas_per_sm));
+    switch (sh.cpt) {
+    case 1: k_batch<1><<<grid, sh.threads, 0, b->stream>>>(b->d_hdr, b->d_tab, s, base); break;
+    case 2: k_batch<2><<<grid, sh.threads, 0, b->stream>>>(b->d_hdr, b->d_tab, s, base); break;
+    case 4: k_batch<4><<<grid, sh.threads, 0, b->stream>>>(b->d_hdr, b->d_tab, s, base); break;
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+// Steps a member still owes before its limit.
+int64_t owed(const imex_batch* b, size_t m, int64_t want)
+{
+    if (b->limit[m] < 0) return want;
+    const int64_t left = b->limit[m] - b->members[m]->steps;
+    return left < 0 ? 0 : (left < want ? left : want);
+}
+
+// Write the member table for a tick where member m runs steps[m] fused
+// steps, and upload it (stream-ordered).
+int upload_table(imex_batch* b, const std::vector<int>& steps)
+{
+    unsigned long long begin = 0;
+    int n = 0;
+    for (size_t m = 0; m < b->members.size(); ++m) {
+        imex_lattice* h = b->members[m];
+        BatchEntry& e = b->h_tab[n++];
+        e.begin = begin;
+        e.plane = h->ncells;
+        e.buf[0] = h->buf[0];
+        e.buf[1] = h->buf[1];
+        e.nx = h->g.nx;
+        e.ny = h->g.ny;
+        e.nz = h->g.nz;
+        e.prec = h->precision;
+        e.cur = h->cur;
+        e.steps = steps[m];
+        e.eps = h->cf32.eps;
+        e.sr = h->cf32.sr;
+        e.seed = (uint32_t)h->steps;
+        e.pad = 0;
+        begin += h->ncells;
+    }
+    b->h_hdr->total = begin;
+    b->h_hdr->count = n;
+    B_CUDA(b, cudaMemcpyAsync(b->d_tab, b->h_tab, sizeof(BatchEntry) * (n ? n : 1), cudaMemcpyHostToDevice, b->stream),
+           "cudaMemcpyAsync");
+    B_CUDA(b, cudaMemcpyAsync(b->d_hdr, b->h_hdr, sizeof(BatchHeader), cudaMemcpyHostToDevice, b->stream),
+           "cudaMemcpyAsync");
+    // the pinned staging is reused next tick: wait until the copies are done
+    B_CUDA(b, cudaStreamSynchronize(b->stream), "cudaStreamSynchronize");
+    return IMEX_OK;
+}
+
+// Make the batch stream wait for every member's queued work.
+int join_members(imex_batch* b)
+{
+    for (imex_lattice* h : b->members) {
+        B_CUDA(b, cudaEventRecord(b->done, h->stream), "cudaEventRecord");
+        B_CUDA(b, cudaStreamWaitEvent(b->stream, b->done, 0), "cudaStreamWaitEvent");
+    }
+    return IMEX_OK;
+}
+
+// Make every member stream wait for the batch stream.
+int release_members(imex_batch* b)
+{
+    B_CUDA(b, cudaEventRecord(b->done, b->stream), "cudaEventRecord");
+    for (imex_lattice* h : b->members) B_CUDA(b, cudaStreamWaitEvent(h->stream, b->done, 0), "cudaStreamWaitEvent");
+    return IMEX_OK;
+}
+
+std::vector<BatchShape> candidates()
+{
+    std::vector<BatchShape> out;
+    const int threads[2] = {128, 256};
+    const int cpts[3] = {1, 2, 4};
+    const int ctas[3] = {2, 4, 8};
+    for (int t : threads)
+        for (int c : cpts)
+            for (int k : ctas) {
+                if (t * k > 2048) continue;
+                BatchShape s;
+                s.threads = t;
+                s.cpt = c;
+                s.ctas_per_sm = k;
+                out.push_back(s);
+            }
+    return out;
+}
+
+// Time each candidate shape on the batch (step 0 of a one-step tick reads
+// buf[cur] and writes the other buffer, leaving every member's state as it
+// was) and keep the fastest.
+int tune_batch(imex_batch* b)
+{
+    std::vector<int> one(b->members.size(), 1);
+    int rc = upload_table(b, one);
+    if (rc) return rc;
+    cudaEvent_t e0, e1;
+    B_CUDA(b, cudaEventCreate(&e0), "cudaEventCreate");
+    B_CUDA(b, cudaEventCreate(&e1), "cudaEventCreate");
+    float best = 0.f;
+    BatchShape best_shape;
+    cudaError_t e = cudaSuccess;
+    for (const BatchShape& sh : candidates()) {
+        e = launch_batch(b, sh, 0);  // warm-up
+        for (int r = 0; r < 2 && e == cudaSuccess; ++r) e = launch_batch(b, sh, 0);
+        if (e == cudaSuccess) e = cudaEventRecord(e0, b->stream);
+        for (int r = 0; r < 3 && e == cudaSuccess; ++r) e = launch_batch(b, sh, 0);
+        if (e == cudaSuccess) e = cudaEventRecord(e1, b->stream);
+        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+        float ms = 0.f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+        if (e != cudaSuccess) break;
+        b->launches += 6;
+        if (!best_shape.threads || ms < best) {
+            best = ms;
+            best_shape = sh;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (e != cudaSuccess) return bcuda(b, e, "batch autotune");
+    b->shape = best_shape;
+    return IMEX_OK;
+}
+
+// Capture K launches (s = 0..K-1) of the current shape into a graph.
+int capture_graph(imex_batch* b, int K)
+{
+    if (b->graph) {
+        cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+    }
+    cudaGraph_t g = nullptr;
+    B_CUDA(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+    cudaError_t e = cudaSuccess;
+    for (int s = 0; s < K && e == cudaSuccess; ++s) e = launch_batch(b, b->shape, s);
+    cudaError_t e2 = cudaStreamEndCapture(b->stream, &g);
+    if (e == cudaSuccess) e = e2;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&b->graph, g, 0);
+    if (g) cudaGraphDestroy(g);
+    if (e != cudaSuccess) return bcuda(b, e, "batch graph capture");
+    b->graph_k = K;
+    b->graph_shape = b->shape;
+    return IMEX_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int imex_batch_create(int max_members, imex_batch** out)
+{
+    if (!out) return set_thread_error(IMEX_ERR_ARG, "imex_batch_create: null output");
+    *out = nullptr;
+    if (max_members < 1 || max_members > kBatchMax)
+        return set_thread_error(IMEX_ERR_ARG, "imex_batch_create: max_members must be in [1, 2048]");
+    imex_batch* b = new imex_batch();
+    b->capacity = max_members;
+    cudaError_t e = cudaGetDevice(&b->device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, b->device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_hdr, sizeof(BatchHeader));
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_tab, sizeof(BatchEntry) * max_members);
+    if (e == cudaSuccess) e = cudaMallocHost(&b->h_hdr, sizeof(BatchHeader));
+    if (e == cudaSuccess) e = cudaMallocHost(&b->h_tab, sizeof(BatchEntry) * max_members);
+    if (e != cudaSuccess) {
+        imex_batch_destroy(b);
+        cudaGetLastError();
+        return set_thread_error(IMEX_ERR_CUDA, std::string("imex_batch_create: ") + cudaGetErrorString(e));
+    }
+    b->graph_steps = 16;
+    *out = b;
+    return IMEX_OK;
+}
+
+void imex_batch_destroy(imex_batch* b)
+{
+    if (!b) return;
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    if (b->d_hdr) cudaFree(b->d_hdr);
+    if (b->d_tab) cudaFree(b->d_tab);
+    if (b->h_hdr) cudaFreeHost(b->h_hdr);
+    if (b->h_tab) cudaFreeHost(b->h_tab);
+    if (b->done) cudaEventDestroy(b->done);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+}
+
+int imex_batch_add(imex_batch* b, imex_lattice* h, int64_t max_steps)
+{
+    if (!b || !h) return set_thread_error(IMEX_ERR_ARG, "imex_batch_add: null argument");
+    if (h->precision == IMEX_F64)
+        return bfail(b, IMEX_ERR_ARG, "imex_batch_add: members must use float32 or float16-deviation storage");
+    if (h->tag == kUninit) return bfail(b, IMEX_ERR_STATE, "imex_batch_add: lattice not initialised");
+    if (h->device != b->device) return bfail(b, IMEX_ERR_ARG, "imex_batch_add: lattice is on another device");
+    if (h->ncells >= 0xffffffffull) return bfail(b, IMEX_ERR_ARG, "imex_batch_add: members need fewer than 2^32 cells");
+    if ((int)b->members.size() >= b->capacity) return bfail(b, IMEX_ERR_MEMORY, "imex_batch_add: batch is full");
+    for (imex_lattice* m : b->members)
+        if (m == h) return bfail(b, IMEX_ERR_ARG, "imex_batch_add: lattice already in the batch");
+    b->members.push_back(h);
+    b->limit.push_back(max_steps);
+    return IMEX_OK;
+}
+
+int imex_batch_remove(imex_batch* b, imex_lattice* h)
+{
+    if (!b || !h) return set_thread_error(IMEX_ERR_ARG, "imex_batch_remove: null argument");
+    for (size_t m = 0; m < b->members.size(); ++m)
+        if (b->members[m] == h) {
+            B_CUDA(b, cudaStreamSynchronize(b->stream), "cudaStreamSynchronize");
+            b->members.erase(b->members.begin() + m);
+            b->limit.erase(b->limit.begin() + m);
+            return IMEX_OK;
+        }
+    return bfail(b, IMEX_ERR_ARG, "imex_batch_remove: lattice not in the batch");
+}
+
+int imex_batch_size(const imex_batch* b) { return b ? (int)b->members.size() : -1; }
+
+int imex_batch_step(imex_batch* b, int nsteps)
+{
+    if (!b) return set_thread_error(IMEX_ERR_ARG, "imex_batch_step: null batch");
+    if (nsteps < 0) return bfail(b, IMEX_ERR_ARG, "imex_batch_step: nsteps < 0");
+    if (b->members.empty() || nsteps == 0) return IMEX_OK;
+    B_CUDA(b, cudaSetDevice(b->device), "cudaSetDevice");
+    // Members whose reference f sits in the buffer (just initialised, or
+    // after get_f) take their first Collision alone (in place), then mark
+    // the streaming pending; every further step is a fused batched step.
+    std::vector<int64_t> left(b->members.size());
+    for (size_t m = 0; m < b->members.size(); ++m) {
+        imex_lattice* h = b->members[m];
+        left[m] = owed(b, m, nsteps);
+        if (left[m] > 0 && h->tag == kExact) {
+            int rc = imex_collision(h);
+            if (!rc) rc = imex_streaming(h);
+            if (rc) return bfail(b, rc, std::string("imex_batch_step: ") + imex_last_error(h));
+            --left[m];
+        }
+    }
+    int rc = join_members(b);
+    if (rc) return rc;
+    if (!b->shape.threads) {
+        rc = tune_batch(b);
+        if (rc) return rc;
+    }
+    std::vector<int> tick(b->members.size());
+    for (;;) {
+        int64_t most = 0;
+        for (size_t m = 0; m < left.size(); ++m) most = std::max(most, left[m]);
+        if (most == 0) break;
+        const int K = b->graph_steps > 0 ? b->graph_steps : 1;
+        const int k = (int)std::min<int64_t>(most, K);
+        for (size_t m = 0; m < left.size(); ++m) tick[m] = (int)std::min<int64_t>(left[m], k);
+        rc = upload_table(b, tick);
+        if (rc) return rc;
+        if (b->graph_steps > 0 && k == b->graph_steps) {
+            if (!b->graph || b->graph_k != k || b->graph_shape.threads != b->shape.threads ||
+                b->graph_shape.cpt != b->shape.cpt || b->graph_shape.ctas_per_sm != b->shape.ctas_per_sm) {
+                rc = capture_graph(b, k);
+                if (rc) return rc;
+            }
+            B_CUDA(b, cudaGraphLaunch(b->graph, b->stream), "cudaGraphLaunch");
+        } else {
+            for (int s = 0; s < k; ++s) B_CUDA(b, launch_batch(b, b->shape, s), "batch kernel launch");
+        }
+        b->launches += k;
+        for (size_t m = 0; m < left.size(); ++m) {
+            imex_lattice* h = b->members[m];
+            h->cur ^= tick[m] & 1;
+            h->steps += tick[m];
+            h->launches += tick[m];
+            left[m] -= tick[m];
+        }
+    }
+    return release_members(b);
+}
+
+int imex_batch_synchronize(imex_batch* b)
+{
+    if (!b) return set_thread_error(IMEX_ERR_ARG, "imex_batch_synchronize: null batch");
+    B_CUDA(b, cudaStreamSynchronize(b->stream), "imex_batch_synchronize");
+    return IMEX_OK;
+}
+
+int imex_batch_set_launch(imex_batch* b, int threads, int cells_per_thread, int ctas_per_sm)
+{
+    if (!b) return set_thread_error(IMEX_ERR_ARG, "imex_batch_set_launch: null batch");
+    if (threads == 0) {
+        b->shape = BatchShape{};
+        return IMEX_OK;
+    }
+    if ((threads != 128 && threads != 256) || (cells_per_thread != 1 && cells_per_thread != 2 && cells_per_thread != 4) ||
+        ctas_per_sm < 1 || ctas_per_sm * threads > 2048)
+        return bfail(b, IMEX_ERR_ARG, "imex_batch_set_launch: threads 128|256, cells_per_thread 1|2|4, "
+                                      "ctas_per_sm*threads <= 2048");
+    b->shape.threads = threads;
+    b->shape.cpt = cells_per_thread;
+    b->shape.ctas_per_sm = ctas_per_sm;
+    return IMEX_OK;
+}
+
+int imex_batch_get_launch(imex_batch* b, int out[3])
+{
+    if (!b || !out) return set_thread_error(IMEX_ERR_ARG, "imex_batch_get_launch: null argument");
+    out[0] = b->shape.threads;
+    out[1] = b->shape.cpt;
+    out[2] = b->shape.ctas_per_sm;
+    return IMEX_OK;
+}
+
+int imex_batch_set_graph(imex_batch* b, int steps_per_graph)
+{
+    if (!b || steps_per_graph < 0) return set_thread_error(IMEX_ERR_ARG, "imex_batch_set_graph: bad argument");
+    b->graph_steps = steps_per_graph;
+    return IMEX_OK;
+}
+
+int64_t imex_batch_kernel_launches(const imex_batch* b) { return b ? b->launches : -1; }
+
+const char* imex_batch_last_error(const imex_batch* b) { return b ? b->err.c_str() : imex::thread_error(); }
+
+}  // extern "C"

@@ -3,6 +3,8 @@
 
 #include <cuda_runtime.h>
 
+#include <cstdint>
+
 #include "imexlbm.h"
 #include "kernels_f64.cuh"
 
@@ -14,6 +16,8 @@ namespace imex {
 struct CollideF32 {
     float eps;
     float w[4], w3[4];
+    int sr;         // float16 storage: 1 stochastic rounding, 0 round to nearest
+    uint32_t seed;  // stochastic-rounding seed of this step
 };
 
 CollideF32 make_collide_f32(double tau0);

@@ -31,6 +31,7 @@
 #include "kernels_fx.cuh"
 #include "kernels_lowp.cuh"
 #include "rows.cuh"
+#include "lattice_internal.hpp"
 
 namespace imex {
 
@@ -44,49 +45,22 @@ int set_thread_error(int code, const std::string& msg)
 
 const char* thread_error() { return g_thread_err.c_str(); }
 
-}  // namespace imex
-
-using namespace imex;
-
-enum Tag { kUninit = 0, kExact = 1, kPendingStream = 2 };
-
-struct imex_lattice {
-    Geom g{};
-    size_t ncells = 0;
-    double tau0 = 0, rho0 = 0, u0 = 0;
-    int precision = IMEX_F64;
-    int engine = IMEX_ENGINE_AUTO;
-    void* buf[2] = {nullptr, nullptr};
-    int cur = 0;
-    Tag tag = kUninit;
-    int64_t steps = 0;
-    int64_t launches = 0;
-    cudaStream_t own_stream = nullptr;
-    cudaStream_t stream = nullptr;
-    int device = 0;
-    double* d_partial = nullptr;  // conserved partials (5 per block)
-    double* d_out = nullptr;      // 5 reduced values
-    double* h_out = nullptr;      // pinned copy of d_out
-    unsigned long long* d_fallback = nullptr;  // fixed-point engine fallback counter
-    size_t bytes = 0;
-    CollideF64 cf64{};
-    CollideF32 cf32{};
-    FxParams fx{};
-    bool fx_ok = false;  // fixed-point engine usable for this lattice
-    unsigned* d_err = nullptr;  // set by kernels whose bounded waits ran out
-    RowConfig rows{};           // launch shape of the fused step (stages 0: one thread per cell)
-    int shape_mode = -1;        // -1 autotune on first use, 0 one thread per cell, 1 row-staged
-    std::string err;
-};
-
-namespace {
-
-int fail(imex_lattice* h, int code, const std::string& msg)
+int lattice_fail(imex_lattice* h, int code, const std::string& msg)
 {
     if (h) h->err = msg;
     set_thread_error(code, msg);
     return code;
 }
+
+size_t lattice_elem_size(int precision) { return precision == IMEX_F64 ? 8 : precision == IMEX_F32 ? 4 : 2; }
+
+}  // namespace imex
+
+using namespace imex;
+
+namespace {
+
+int fail(imex_lattice* h, int code, const std::string& msg) { return lattice_fail(h, code, msg); }
 
 int cuda_fail(imex_lattice* h, cudaError_t e, const char* what)
 {
@@ -100,7 +74,7 @@ int cuda_fail(imex_lattice* h, cudaError_t e, const char* what)
         if (e_ != cudaSuccess) return cuda_fail(h, e_, what); \
     } while (0)
 
-size_t elem_size(int precision) { return precision == IMEX_F64 ? 8 : precision == IMEX_F32 ? 4 : 2; }
+size_t elem_size(int precision) { return lattice_elem_size(precision); }
 
 bool use_fixed(const imex_lattice* h)
 {
@@ -161,9 +135,10 @@ std::vector<RowConfig> row_candidates(const imex_lattice* h)
 std::mutex g_tune_lock;
 std::map<std::tuple<int, int, int, int, int>, RowConfig> g_tune_cache;
 
+// (precision, engine or rounding mode, nx, ny, nz)
 std::tuple<int, int, int, int, int> tune_key(const imex_lattice* h)
 {
-    return std::make_tuple(h->precision, use_fixed(h) ? 1 : 0, h->g.nx, h->g.ny, h->g.nz);
+    return std::make_tuple(h->precision, (use_fixed(h) ? 1 : 0) + 2 * h->cf32.sr, h->g.nx, h->g.ny, h->g.nz);
 }
 
 cudaError_t launch_fused_rows(imex_lattice* h, const void* src, void* dst, const RowConfig& rc)
@@ -193,18 +168,25 @@ int time_shape(imex_lattice* h, const RowConfig& rc, float* ms)
     IMEX_CUDA(h, cudaEventCreate(&e1), "cudaEventCreate");
     cudaError_t e = cudaSuccess;
     const int reps = 3;
-    for (int r = 0; r <= reps && e == cudaSuccess; ++r) {
-        if (r == 1) e = cudaEventRecord(e0, h->stream);
-        if (e == cudaSuccess) e = rc.stages > 0 ? launch_fused_rows(h, src, dst, rc) : launch_fused_classic(h, src, dst);
-        if (e == cudaSuccess) h->launches++;
+    float best = 0.f;
+    // one warm-up launch, then the faster of two timed rounds of `reps`
+    e = rc.stages > 0 ? launch_fused_rows(h, src, dst, rc) : launch_fused_classic(h, src, dst);
+    for (int round = 0; round < 2 && e == cudaSuccess; ++round) {
+        e = cudaEventRecord(e0, h->stream);
+        for (int r = 0; r < reps && e == cudaSuccess; ++r) {
+            e = rc.stages > 0 ? launch_fused_rows(h, src, dst, rc) : launch_fused_classic(h, src, dst);
+            if (e == cudaSuccess) h->launches++;
+        }
+        if (e == cudaSuccess) e = cudaEventRecord(e1, h->stream);
+        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+        float t = 0.f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&t, e0, e1);
+        if (e == cudaSuccess && (round == 0 || t < best)) best = t;
     }
-    if (e == cudaSuccess) e = cudaEventRecord(e1, h->stream);
-    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
-    if (e == cudaSuccess) e = cudaEventElapsedTime(ms, e0, e1);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (e != cudaSuccess) return cuda_fail(h, e, "autotune");
-    *ms /= reps;
+    *ms = best / reps;
     return IMEX_OK;
 }
 
@@ -272,6 +254,7 @@ int launch_mode(imex_lattice* h, int mode)
         int rc = ensure_tuned(h);
         if (rc) return rc;
     }
+    h->cf32.seed = (uint32_t)h->steps;  // stochastic rounding: a new stream of bits every step
     if (mode == kModeFused && h->rows.stages > 0)
         e = launch_fused_rows(h, src, dst, h->rows);
     else if (lowp(h))
@@ -351,6 +334,7 @@ int imex_create(int nx, int ny, int nz, double tau, double rho0, double u0, int 
     h->precision = precision;
     h->cf64 = make_collide_f64(tau);
     h->cf32 = make_collide_f32(tau);
+    h->cf32.sr = precision == IMEX_F16DEV;  // float16 deviations: stochastic rounding by default
     h->fx_ok = make_fx_params(tau, rho0, &h->fx);
 
     auto bail = [&](int code) {
@@ -409,9 +393,14 @@ void imex_destroy(imex_lattice* h)
     delete h;
 }
 
-int imex_initialize(imex_lattice* h)
+int imex_initialize(imex_lattice* h) { return imex_initialize_phase(h, 0.0, 0.0, 0.0); }
+
+int imex_initialize_phase(imex_lattice* h, double phx, double phy, double phz)
 {
     if (!h) return set_thread_error(IMEX_ERR_ARG, "imex_initialize: null handle");
+    if (!std::isfinite(phx) || !std::isfinite(phy) || !std::isfinite(phz))
+        return fail(h, IMEX_ERR_ARG, "imex_initialize_phase: phases must be finite");
+    const double phase[3] = {phx, phy, phz};
     IMEX_CUDA(h, cudaSetDevice(h->device), "cudaSetDevice");
     // Per-axis trigonometric tables, src/lbm.cpp:81-93:
     //   x = (double)(i - ghost + x_lo) / (double)glx * 2.0 * pi, pi = 3.1415926
@@ -424,7 +413,7 @@ int imex_initialize(imex_lattice* h)
     for (int d = 0; d < 3; ++d) {
         offs[d] = off;
         for (int i = 0; i < n[d]; ++i) {
-            const double xx = (double)i / (double)n[d] * 2.0 * 3.1415926;
+            const double xx = (double)i / (double)n[d] * 2.0 * 3.1415926 + phase[d];
             host[off++] = std::sin(xx);
             host[off++] = std::cos(xx);
             host[off++] = std::cos(2.0 * xx);
@@ -662,6 +651,20 @@ int imex_set_engine(imex_lattice* h, int engine)
     return IMEX_OK;
 }
 
+int imex_set_rounding(imex_lattice* h, int mode)
+{
+    if (!h) return set_thread_error(IMEX_ERR_ARG, "imex_set_rounding: null handle");
+    if (mode != IMEX_ROUND_NEAREST && mode != IMEX_ROUND_STOCHASTIC)
+        return fail(h, IMEX_ERR_ARG, "imex_set_rounding: unknown mode");
+    if (mode == IMEX_ROUND_STOCHASTIC && h->precision != IMEX_F16DEV)
+        return fail(h, IMEX_ERR_ARG, "imex_set_rounding: stochastic rounding applies to IMEX_F16DEV storage");
+    const int sr = mode == IMEX_ROUND_STOCHASTIC;
+    // a shape the autotuner chose for the other rounding mode is re-chosen
+    if (sr != h->cf32.sr && !h->shape_pinned) h->shape_mode = -1;
+    h->cf32.sr = sr;
+    return IMEX_OK;
+}
+
 int imex_set_stream(imex_lattice* h, void* s)
 {
     if (!h) return set_thread_error(IMEX_ERR_ARG, "imex_set_stream: null handle");
@@ -681,11 +684,13 @@ int imex_set_launch(imex_lattice* h, int stages, int rows_per_stage, int ctas_pe
     if (!h) return set_thread_error(IMEX_ERR_ARG, "imex_set_launch: null handle");
     if (stages < 0) {
         h->shape_mode = -1;
+        h->shape_pinned = false;
         return IMEX_OK;
     }
     if (stages == 0) {
         h->rows = RowConfig{};
         h->shape_mode = 0;
+        h->shape_pinned = true;
         return IMEX_OK;
     }
     if (!rows_eligible_for(h))
@@ -702,6 +707,7 @@ int imex_set_launch(imex_lattice* h, int stages, int rows_per_stage, int ctas_pe
     rc.threads = h->g.nz >= 256 ? 256 : ((h->g.nz + 31) / 32) * 32;
     h->rows = rc;
     h->shape_mode = 1;
+    h->shape_pinned = true;
     return IMEX_OK;
 }
 

@@ -1,0 +1,61 @@
+// Internal layout of a lattice handle (struct imex_lattice of the C ABI),
+// shared by the translation units that drive its buffers.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+
+#include "kernels_f64.cuh"
+#include "kernels_fx.cuh"
+#include "kernels_lowp.cuh"
+#include "rows.cuh"
+
+using imex::CollideF32;
+using imex::CollideF64;
+using imex::FxParams;
+using imex::Geom;
+using imex::RowConfig;
+
+// kExact: the device buffer is the reference's f.  kPendingStream: the
+// reference's f is S(buffer) (the last streaming is not applied yet).
+enum Tag { kUninit = 0, kExact = 1, kPendingStream = 2 };
+
+struct imex_lattice {
+    Geom g{};
+    size_t ncells = 0;
+    double tau0 = 0, rho0 = 0, u0 = 0;
+    int precision = IMEX_F64;
+    int engine = IMEX_ENGINE_AUTO;
+    void* buf[2] = {nullptr, nullptr};
+    int cur = 0;
+    Tag tag = kUninit;
+    int64_t steps = 0;
+    int64_t launches = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    int device = 0;
+    double* d_partial = nullptr;  // conserved partials (5 per block)
+    double* d_out = nullptr;      // 5 reduced values
+    double* h_out = nullptr;      // pinned copy of d_out
+    unsigned long long* d_fallback = nullptr;  // fixed-point engine fallback counter
+    size_t bytes = 0;
+    CollideF64 cf64{};
+    CollideF32 cf32{};
+    FxParams fx{};
+    bool fx_ok = false;  // fixed-point engine usable for this lattice
+    unsigned* d_err = nullptr;  // set by kernels whose bounded waits ran out
+    RowConfig rows{};           // launch shape of the fused step (stages 0: one thread per cell)
+    int shape_mode = -1;        // -1 autotune on first use, 0 one thread per cell, 1 row-staged
+    bool shape_pinned = false;  // shape set by imex_set_launch rather than the autotuner
+    std::string err;
+};
+
+namespace imex {
+
+// Both defined in lattice.cu.
+int lattice_fail(imex_lattice* h, int code, const std::string& msg);
+size_t lattice_elem_size(int precision);
+
+}  // namespace imex

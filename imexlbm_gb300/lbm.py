@@ -93,6 +93,10 @@ class LBM:
     def Initialize(self) -> None:
         self._check(self._L.imex_initialize(self._h))
 
+    def initialize_phase(self, phx: float, phy: float, phz: float) -> None:
+        """Taylor-Green init with coordinates shifted by (phx, phy, phz)."""
+        self._check(self._L.imex_initialize_phase(self._h, float(phx), float(phy), float(phz)))
+
     def Collision(self) -> None:
         self._check(self._L.imex_collision(self._h))
 
@@ -157,6 +161,10 @@ class LBM:
         self._check(self._L.imex_get_launch(self._h, out))
         return tuple(out)
 
+    def set_rounding(self, mode: int) -> None:
+        """IMEX_ROUND_NEAREST or IMEX_ROUND_STOCHASTIC (float16-deviation storage)."""
+        self._check(self._L.imex_set_rounding(self._h, int(mode)))
+
     def set_stream(self, stream_ptr: int | None) -> None:
         self._check(self._L.imex_set_stream(self._h, ctypes.c_void_p(stream_ptr or 0)))
 
@@ -178,4 +186,66 @@ class LBM:
         return int(self._L.imex_device_bytes(self._h))
 
 
-__all__ = ["System", "LBM", "ImexError", "Q"]
+class Batch:
+    """Float32 / float16-deviation lattices advanced together by one
+    persistent launch per step (include/imexlbm.h, imex_batch_*)."""
+
+    def __init__(self, max_members: int = 256):
+        self._L = _lib.load()
+        b = ctypes.c_void_p()
+        check(self._L.imex_batch_create(int(max_members), ctypes.byref(b)))
+        self._b = b
+        self.members = []
+
+    def _check(self, rc: int) -> None:
+        if rc != _lib.IMEX_OK:
+            msg = self._L.imex_batch_last_error(self._b)
+            raise ImexError(rc, msg.decode() if msg else "")
+
+    def add(self, lat: LBM, max_steps: int = -1) -> None:
+        self._check(self._L.imex_batch_add(self._b, lat.handle, int(max_steps)))
+        self.members.append(lat)
+
+    def remove(self, lat: LBM) -> None:
+        self._check(self._L.imex_batch_remove(self._b, lat.handle))
+        self.members.remove(lat)
+
+    def step(self, n: int) -> None:
+        self._check(self._L.imex_batch_step(self._b, int(n)))
+
+    def synchronize(self) -> None:
+        self._check(self._L.imex_batch_synchronize(self._b))
+
+    def set_launch(self, threads: int, cells_per_thread: int = 1, ctas_per_sm: int = 4) -> None:
+        self._check(self._L.imex_batch_set_launch(self._b, int(threads), int(cells_per_thread), int(ctas_per_sm)))
+
+    def get_launch(self):
+        out = (ctypes.c_int * 3)()
+        self._check(self._L.imex_batch_get_launch(self._b, out))
+        return tuple(out)
+
+    def set_graph(self, steps: int) -> None:
+        self._check(self._L.imex_batch_set_graph(self._b, int(steps)))
+
+    def kernel_launches(self) -> int:
+        return int(self._L.imex_batch_kernel_launches(self._b))
+
+    def close(self) -> None:
+        if getattr(self, "_b", None):
+            self._L.imex_batch_destroy(self._b)
+            self._b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+__all__ = ["System", "LBM", "Batch", "ImexError", "Q"]

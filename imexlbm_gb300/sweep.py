@@ -5,7 +5,8 @@ Default workload: 512^3, Re = 1600, u0 = 0.05, 2000 steps, reporting every
 100 - three runs side by side:
   (a) float64 storage (the reference's precision; fixed-point engine),
   (b) float32 storage, float32 collision,
-  (c) float16 storage of f - w, float32 collision.
+  (c) float16 storage of f - w, float32 collision, rounded to nearest,
+  (d) the same with stochastic rounding.
 Every report step prints, for (b) and (c) against (a): the relative
 kinetic-energy error, the largest velocity difference over all cells (in
 units of u0) and the relative mass drift of each run; at the end, each
@@ -14,7 +15,7 @@ Mass, momentum and ke are float64 reductions in every run.
 
 Usage: python -m imexlbm_gb300.sweep [--size 512] [--steps 2000] [--report 100]
                                      [--re 1600] [--u0 0.05] [--json out.json]
-Needs about 27 x 14 bytes per cell of device memory (101 GB at 512^3).
+Needs about 27 x 18 bytes per cell of device memory (130 GB at 512^3).
 """
 from __future__ import annotations
 
@@ -32,18 +33,21 @@ def run(size=512, steps=2000, report=100, re=1600, u0=0.05, out=None, log=print)
     import torch
 
     deck = System(text=f"1.0 0.1 {re}\n{u0} {steps} {report}\n{size} {size} {size}\n")
-    names = [("f64", _lib.IMEX_F64), ("f32", _lib.IMEX_F32), ("f16dev", _lib.IMEX_F16DEV)]
+    names = [("f64", _lib.IMEX_F64), ("f32", _lib.IMEX_F32), ("f16dev", _lib.IMEX_F16DEV),
+             ("f16dev_sr", _lib.IMEX_F16DEV)]
     lats, streams = {}, {}
     for name, prec in names:
         streams[name] = torch.cuda.Stream()
         lat = LBM(size, size, size, deck.tau, deck.rho0, deck.u0, precision=prec)
         lat.set_stream(streams[name].cuda_stream)
+        lat.set_rounding(_lib.IMEX_ROUND_STOCHASTIC if name.endswith("_sr") else _lib.IMEX_ROUND_NEAREST)
         lat.Initialize()
         lats[name] = lat
     m0 = {k: v.Conserved()[0] for k, v in lats.items()}
     ms = {k: 0.0 for k in lats}
     rows = []
-    worst = {k: {"ke_rel": 0.0, "u_max_over_u0": 0.0, "mass_drift_rel": 0.0} for k in ("f32", "f16dev")}
+    low = [n for n, _ in names if n != "f64"]
+    worst = {k: {"ke_rel": 0.0, "u_max_over_u0": 0.0, "mass_drift_rel": 0.0} for k in low}
     done = 0
     while done < steps:
         k = min(report, steps - done)
@@ -58,7 +62,7 @@ def run(size=512, steps=2000, report=100, re=1600, u0=0.05, out=None, log=print)
         done += k
         cons = {name: lat.Conserved() for name, lat in lats.items()}
         row = {"step": done, "ke_f64": cons["f64"][4]}
-        for name in ("f32", "f16dev"):
+        for name in low:
             ke_rel = abs(cons[name][4] - cons["f64"][4]) / cons["f64"][4]
             du, _ = lats[name].velocity_max_diff(lats["f64"])
             drift = abs(cons[name][0] - m0[name]) / m0[name]

@@ -40,6 +40,11 @@ extern "C" {
 #define IMEX_F32 1    /* float32 storage, float32 collision                     */
 #define IMEX_F16DEV 2 /* float16 storage of f_a - w_a, float32 collision        */
 
+/* Rounding of float16-deviation storage (imex_set_rounding). */
+#define IMEX_ROUND_NEAREST 0    /* round to nearest even                               */
+#define IMEX_ROUND_STOCHASTIC 1 /* round up or down with probabilities that keep the
+                                   expected stored value exact                          */
+
 /* Arithmetic engine of the float64 collision. */
 #define IMEX_ENGINE_AUTO 0   /* fastest engine that meets float64 parity            */
 #define IMEX_ENGINE_NATIVE 1 /* native float64 FMA arithmetic                       */
@@ -83,6 +88,12 @@ void imex_destroy(imex_lattice *h);
 /* Taylor-Green initial field and equilibrium distributions.
  * Replaces LBM::Initialize() (src/lbm.cpp:38-111). */
 int imex_initialize(imex_lattice *h);
+
+/* Taylor-Green initial field with the coordinates shifted by a phase per
+ * axis: x = i / nx * 2 pi + phx (and likewise y, z) in src/lbm.cpp:81-93.
+ * imex_initialize is the zero-phase case.  Used to give the lattices of a
+ * batch distinct flows; no counterpart in the reference. */
+int imex_initialize_phase(imex_lattice *h, double phx, double phy, double phz);
 
 /* BGK collision with relaxation rate 1/(tau0 + 0.5).
  * Replaces LBM::Collision() (src/lbm.cpp:131-166). */
@@ -172,6 +183,16 @@ int imex_get_launch(imex_lattice *h, int out[4]);
 /* Select the float64 arithmetic engine (IMEX_ENGINE_*).  Default AUTO. */
 int imex_set_engine(imex_lattice *h, int engine);
 
+/* Rounding mode of IMEX_F16DEV storage (default IMEX_ROUND_STOCHASTIC).  At
+ * omega close to 2 (high Reynolds number) the non-equilibrium part of each
+ * population is far below half a float16 step of f - w, so rounding to
+ * nearest erases it deterministically and biases the viscous decay (512^3,
+ * Re 1600: kinetic energy off by 9e-8 per step); stochastic rounding keeps
+ * it in expectation (4e-9 after 1000 steps) at some throughput.  The random
+ * bits come from a hash of (cell, step), so runs are reproducible and
+ * identical across kernels and batches. */
+int imex_set_rounding(imex_lattice *h, int mode);
+
 /* Queue the handle's work on an existing CUDA stream (cudaStream_t passed as
  * void*; NULL restores the handle's own stream). */
 int imex_set_stream(imex_lattice *h, void *cuda_stream);
@@ -196,6 +217,50 @@ size_t imex_device_bytes(const imex_lattice *h);
 /* Last error message of the handle (or of the calling thread when h is
  * NULL, for errors raised before a handle exists).  Never NULL. */
 const char *imex_last_error(const imex_lattice *h);
+
+/* ---------------------------------------------------------------- batch -- */
+
+/* Many float32 / float16-deviation lattices of any sizes, advanced together
+ * by one persistent kernel launch per step over a packed cell index (no
+ * counterpart in the reference, which runs one lattice per process).  The
+ * batch holds handles created by imex_create; each member keeps its own
+ * buffers, state, diagnostics (imex_conserved, imex_get_f ...) and
+ * results identical bit for bit to stepping it alone.  Steps run on the
+ * batch's own stream in CUDA graphs of K launches (imex_batch_set_graph);
+ * the members' streams are ordered before and after each imex_batch_step.
+ * Calls on one batch are not thread-safe. */
+typedef struct imex_batch imex_batch;
+
+/* Create an empty batch for up to max_members (<= 2048) lattices. */
+int imex_batch_create(int max_members, imex_batch **out);
+void imex_batch_destroy(imex_batch *b);
+
+/* Add an initialised float32 / float16-deviation lattice (fewer than 2^32
+ * cells).  max_steps >= 0 stops the member once imex_steps_done reaches it
+ * (its later imex_batch_step calls skip it); -1 for no limit. */
+int imex_batch_add(imex_batch *b, imex_lattice *h, int64_t max_steps);
+int imex_batch_remove(imex_batch *b, imex_lattice *h);
+int imex_batch_size(const imex_batch *b);
+
+/* Advance every member nsteps reference steps (Collision then Streaming,
+ * as imex_step), or up to its limit.  The first call times the launch
+ * shapes (threads per CTA, cells per thread, CTAs per SM) on the batch
+ * itself, without changing any member's state, and keeps the fastest. */
+int imex_batch_step(imex_batch *b, int nsteps);
+int imex_batch_synchronize(imex_batch *b);
+
+/* Pin the launch shape (threads 128|256, cells_per_thread 1|2|4,
+ * ctas_per_sm * threads <= 2048), or threads = 0 to retune. */
+int imex_batch_set_launch(imex_batch *b, int threads, int cells_per_thread, int ctas_per_sm);
+int imex_batch_get_launch(imex_batch *b, int out[3]);
+
+/* Steps per captured CUDA graph (default 16; 0 launches each step
+ * directly). */
+int imex_batch_set_graph(imex_batch *b, int steps_per_graph);
+
+/* Kernel launches issued by the batch (one per batched step). */
+int64_t imex_batch_kernel_launches(const imex_batch *b);
+const char *imex_batch_last_error(const imex_batch *b);
 
 /* Library version string. */
 const char *imex_version(void);

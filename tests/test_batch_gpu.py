@@ -1,0 +1,129 @@
+"""Batched step: many uneven reduced-precision lattices in one persistent
+launch per step.  The batched kernel runs the per-cell arithmetic of the
+one-lattice kernels, so every member must end bit-identical to the same
+lattice stepped alone - whatever the batch's size mix, launch shape, graph
+length, or the members joining, leaving and finishing in between."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+SPECS = [  # shape, precision name, tau, u0, phase
+    ((16, 16, 16), "f32", 0.004, 0.05, (0.0, 0.0, 0.0)),
+    ((24, 20, 12), "f16dev", 0.02, 0.06, (0.3, 1.1, 2.0)),
+    ((32, 32, 32), "f32", 0.0007, 0.04, (1.0, 0.5, 0.25)),
+    ((17, 9, 13), "f16dev", 0.01, 0.07, (2.5, 0.1, 4.0)),
+    ((8, 8, 8), "f32", 0.1, 0.03, (0.0, 3.0, 1.0)),
+    ((1, 5, 40), "f32", 0.05, 0.05, (0.7, 0.7, 0.7)),
+]
+
+
+def prec(imex, name):
+    return {"f32": imex.IMEX_F32, "f16dev": imex.IMEX_F16DEV}[name]
+
+
+def make(imex, spec):
+    shape, pname, tau, u0, ph = spec
+    lat = imex.LBM(*shape, tau, 1.0, u0, precision=prec(imex, pname))
+    lat.initialize_phase(*ph)
+    return lat
+
+
+def alone(imex, spec, steps):
+    with make(imex, spec) as lat:
+        lat.step(steps)
+        return lat.get_f()
+
+
+def test_batch_equals_alone(imex):
+    steps = 23
+    want = [alone(imex, s, steps) for s in SPECS]
+    lats = [make(imex, s) for s in SPECS]
+    with imex.Batch(16) as b:
+        for lat in lats:
+            b.add(lat)
+        b.step(10)
+        b.step(13)
+        for lat, w in zip(lats, want):
+            assert lat.steps_done() == steps
+            assert np.array_equal(lat.get_f(), w)
+        assert b.kernel_launches() >= steps - 1
+    for lat in lats:
+        lat.close()
+
+
+@pytest.mark.parametrize("shape", [(128, 1, 1), (256, 2, 4), (128, 4, 8), (256, 1, 2)])
+@pytest.mark.parametrize("graph", [0, 5])
+def test_batch_launch_shapes_and_graphs(imex, shape, graph):
+    steps = 12
+    want = [alone(imex, s, steps) for s in SPECS[:4]]
+    lats = [make(imex, s) for s in SPECS[:4]]
+    with imex.Batch(8) as b:
+        b.set_launch(*shape)
+        b.set_graph(graph)
+        for lat in lats:
+            b.add(lat)
+        b.step(steps)
+        for lat, w in zip(lats, want):
+            assert np.array_equal(lat.get_f(), w)
+    for lat in lats:
+        lat.close()
+
+
+def test_members_join_leave_and_finish(imex):
+    """Continuous batching: members admitted and retired between steps, with
+    per-member step limits, each ending where it would alone."""
+    limits = {0: 7, 1: 30, 2: -1, 3: 18}
+    lats = [make(imex, s) for s in SPECS[:5]]
+    with imex.Batch(8) as b:
+        b.set_graph(4)
+        b.add(lats[0], limits[0])
+        b.add(lats[1], limits[1])
+        b.step(5)                     # 0 and 1 at 5
+        b.add(lats[2], limits[2])     # joins at step 0
+        b.add(lats[3], limits[3])
+        b.step(6)                     # 0 stops at 7; 1 at 11; 2, 3 at 6
+        b.remove(lats[2])
+        lats[2].step(3)               # leaves and continues alone: 9
+        b.add(lats[4])                # joins
+        b.step(20)                    # 1 at 30 (limit), 3 at 18 (limit), 4 at 20
+        b.add(lats[2])
+        b.step(4)                     # 2 at 13, 4 at 24
+    expect = [7, 30, 13, 18, 24]
+    for i, lat in enumerate(lats):
+        assert lat.steps_done() == expect[i], (i, lat.steps_done())
+        assert np.array_equal(lat.get_f(), alone(imex, SPECS[i], expect[i])), i
+        lat.close()
+
+
+def test_batch_member_diagnostics_match_alone(imex):
+    spec = SPECS[2]
+    with make(imex, spec) as ref:
+        ref.step(15)
+        want = ref.Conserved()
+    with make(imex, spec) as lat, imex.Batch(2) as b:
+        b.add(lat)
+        b.step(15)
+        assert lat.Conserved() == want
+
+
+def test_batch_stochastic_rounding_equals_alone(imex):
+    spec = SPECS[1]
+    with make(imex, spec) as ref:
+        ref.set_rounding(imex.IMEX_ROUND_STOCHASTIC)
+        ref.step(17)
+        want = ref.get_f()
+    with make(imex, spec) as lat, make(imex, SPECS[0]) as other, imex.Batch(4) as b:
+        lat.set_rounding(imex.IMEX_ROUND_STOCHASTIC)
+        b.set_graph(5)
+        b.add(other)
+        b.add(lat)
+        b.step(17)
+        assert np.array_equal(lat.get_f(), want)
+
+
+def test_batch_rejects_float64(imex):
+    with imex.LBM(8, 8, 8, 0.1, 1.0, 0.05) as lat, imex.Batch(2) as b:
+        lat.Initialize()
+        with pytest.raises(imex.ImexError):
+            b.add(lat)

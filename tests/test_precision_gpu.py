@@ -117,3 +117,44 @@ def test_fixed_engine_refuses_low_precision(imex):
     with imex.LBM(4, 4, 4, 0.1, 1.0, 0.05, precision=imex.IMEX_F32) as lat:
         with pytest.raises(imex.ImexError):
             lat.set_engine(imex.IMEX_ENGINE_FIXED)
+
+
+def test_stochastic_rounding_is_deterministic_and_kernel_independent(imex):
+    """Stochastic rounding draws its bits from (cell, step): two runs agree
+    bit for bit, and so do the one-thread-per-cell and row-staged kernels."""
+    shape = (16, 12, 32)
+    runs = []
+    for stages, rows in [(0, 1), (0, 1), (2, 4)]:
+        with imex.LBM(*shape, 0.002, 1.0, 0.05, precision=imex.IMEX_F16DEV) as lat:
+            lat.set_rounding(imex.IMEX_ROUND_STOCHASTIC)
+            lat.set_launch(stages, rows, 1)
+            lat.Initialize()
+            lat.step(21)
+            runs.append(lat.get_f())
+    assert np.array_equal(runs[0], runs[1])
+    assert np.array_equal(runs[0], runs[2])
+    with imex.LBM(*shape, 0.002, 1.0, 0.05, precision=imex.IMEX_F16DEV) as lat:
+        lat.Initialize()
+        lat.step(21)
+        assert not np.array_equal(lat.get_f(), runs[0])   # nearest rounding differs
+
+
+def test_stochastic_rounding_keeps_ke_on_the_deck(imex, oracle):
+    d = oracle.parse_deck("1.0 0.1 1600\n0.05 100 10\n32 32 32\n")
+    f = oracle.init(32, 32, 32, d.rho0, d.u0)
+    with imex.LBM(32, 32, 32, d.tau, d.rho0, d.u0, precision=imex.IMEX_F16DEV) as lat:
+        lat.set_rounding(imex.IMEX_ROUND_STOCHASTIC)
+        lat.Initialize()
+        m0 = lat.Conserved()[0]
+        lat.step(100)
+        oracle.step(f, d.tau, 100)
+        c = lat.Conserved()
+    w = oracle.conserved(f)
+    assert abs(c[4] - w[4]) <= 1e-4 * w[4]
+    assert abs(c[0] - m0) <= 1e-6 * m0
+
+
+def test_stochastic_rounding_needs_float16(imex):
+    with imex.LBM(4, 4, 4, 0.1, 1.0, 0.05, precision=imex.IMEX_F32) as lat:
+        with pytest.raises(imex.ImexError):
+            lat.set_rounding(imex.IMEX_ROUND_STOCHASTIC)
