@@ -204,7 +204,7 @@ def parse_deck_text(n):
 def workload_config(a, engine):
     prec = getattr(a, "precision", "f64")
     desc = {"f64": "float64 distributions", "f32": "float32 distributions",
-            "f16dev": "float16 deviations f - w"}[prec]
+            "f16dev": "float16 deviations 2^12 (f - w)"}[prec]
     esize = {"f64": 8, "f32": 4, "f16dev": 2}[prec]
     if prec == "f16dev":
         desc += ", %s rounding" % getattr(a, "rounding", "nearest")

@@ -18,6 +18,7 @@ IMEX_ERR_MEMORY = 3
 IMEX_ERR_DECK = 4
 IMEX_ERR_NONFINITE = 5
 IMEX_ERR_STATE = 6
+IMEX_ERR_IO = 7
 
 IMEX_F64 = 0
 IMEX_F32 = 1
@@ -35,6 +36,18 @@ _dp = ctypes.POINTER(ctypes.c_double)
 _h = ctypes.c_void_p
 
 
+IMEX_PHASE_COLLISION = 0
+IMEX_PHASE_STREAM = 1
+IMEX_PHASE_MACRO = 2
+IMEX_PHASE_CONSERVED = 3
+IMEX_NPHASE = 4
+
+
+class PhaseStats(ctypes.Structure):
+    _fields_ = [("calls", ctypes.c_int64), ("total_ms", ctypes.c_double), ("min_ms", ctypes.c_double),
+                ("max_ms", ctypes.c_double)]
+
+
 class Deck(ctypes.Structure):
     """struct imex_deck (include/imexlbm.h)."""
 
@@ -45,6 +58,31 @@ class Deck(ctypes.Structure):
         ("cs2", ctypes.c_double), ("cs", ctypes.c_double), ("Ma", ctypes.c_double),
         ("miu", ctypes.c_double), ("tau", ctypes.c_double),
     ]
+
+
+class Request(ctypes.Structure):
+    """struct imex_request (include/imexlbm.h)."""
+
+    _fields_ = [("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nz", ctypes.c_int),
+                ("precision", ctypes.c_int), ("rounding", ctypes.c_int), ("pad", ctypes.c_int),
+                ("tau", ctypes.c_double), ("rho0", ctypes.c_double), ("u0", ctypes.c_double),
+                ("phase", ctypes.c_double * 3), ("steps", ctypes.c_int64), ("tag", ctypes.c_int64)]
+
+
+class Result(ctypes.Structure):
+    """struct imex_result (include/imexlbm.h)."""
+
+    _fields_ = [("id", ctypes.c_int64), ("tag", ctypes.c_int64), ("status", ctypes.c_int), ("pad", ctypes.c_int),
+                ("conserved", ctypes.c_double * 5), ("steps", ctypes.c_int64), ("cells", ctypes.c_int64),
+                ("t_submit", ctypes.c_double), ("t_admit", ctypes.c_double), ("t_done", ctypes.c_double)]
+
+
+class ServerStats(ctypes.Structure):
+    """struct imex_server_stats (include/imexlbm.h)."""
+
+    _fields_ = [("queued", ctypes.c_int64), ("active", ctypes.c_int64), ("completed", ctypes.c_int64),
+                ("bytes_in_use", ctypes.c_int64), ("cell_updates", ctypes.c_int64), ("ticks", ctypes.c_int64),
+                ("busy_seconds", ctypes.c_double), ("now", ctypes.c_double), ("failed", ctypes.c_int64)]
 
 
 SIGNATURES = {
@@ -60,6 +98,12 @@ SIGNATURES = {
     "imex_conserved": (ctypes.c_int, [_h, _dp]),
     "imex_macroscopic": (ctypes.c_int, [_h, _dp, _dp, _dp, _dp]),
     "imex_velocity_max_diff": (ctypes.c_int, [_h, _h, _dp]),
+    "imex_minmax_uvwp": (ctypes.c_int, [_h, _dp]),
+    "imex_profile_enable": (ctypes.c_int, [_h, ctypes.c_int]),
+    "imex_profile_read": (ctypes.c_int, [_h, ctypes.c_void_p, ctypes.c_int]),
+    "imex_write_tecplot": (ctypes.c_int, [_h, ctypes.c_char_p, ctypes.c_int]),
+    "imex_checkpoint_save": (ctypes.c_int, [_h, ctypes.c_char_p]),
+    "imex_checkpoint_load": (ctypes.c_int, [_h, ctypes.c_char_p]),
     "imex_get_f": (ctypes.c_int, [_h, _dp, ctypes.c_size_t]),
     "imex_set_f": (ctypes.c_int, [_h, _dp, ctypes.c_size_t]),
     "imex_get_f_device": (ctypes.c_int, [_h, ctypes.c_void_p, ctypes.c_size_t]),
@@ -88,9 +132,18 @@ SIGNATURES = {
     "imex_batch_synchronize": (ctypes.c_int, [ctypes.c_void_p]),
     "imex_batch_set_launch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     "imex_batch_get_launch": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]),
+    "imex_batch_set_row_launch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    "imex_batch_get_row_launch": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]),
     "imex_batch_set_graph": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "imex_batch_kernel_launches": (ctypes.c_int64, [ctypes.c_void_p]),
     "imex_batch_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
+    "imex_server_create": (ctypes.c_int, [ctypes.c_size_t, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]),
+    "imex_server_submit": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Request), ctypes.POINTER(ctypes.c_int64)]),
+    "imex_server_poll": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Result), ctypes.c_int,
+                                        ctypes.POINTER(ctypes.c_int)]),
+    "imex_server_get_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ServerStats)]),
+    "imex_server_now": (ctypes.c_double, [ctypes.c_void_p]),
+    "imex_server_destroy": (None, [ctypes.c_void_p]),
 }
 
 _lib = None

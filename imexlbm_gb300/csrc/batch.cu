@@ -18,9 +18,20 @@
 // only while s < its step count for the tick, and within a tick it reads
 // buf[cur ^ (s & 1)] and writes the other buffer.
 //
-// Launch shape (threads per CTA, cells per thread, CTAs per SM) is chosen
-// by an autotuner that times each candidate on the batch itself; timing
-// writes only the members' spare buffers, so it changes no state.
+// Members whose rows suit asynchronous bulk copies (nz * element size a
+// multiple of 16 bytes) run instead in a second persistent kernel, the
+// batched form of the row-staged step (rows.cuh): its work items are blocks
+// of B consecutive y-rows of one member, B chosen per member so that an
+// item's 27 source runs fill one stage of a shared-memory ring; the copies
+// of later items are in flight while an item is collided, and the item's
+// cells are spread over all threads of the CTA whatever the member's nz.
+// Items of members whose step count for the tick is exhausted are armed
+// with no bytes and skipped, keeping the ring's phases uniform.
+//
+// Launch shapes (cell kernel: threads per CTA, cells per thread, CTAs per
+// SM; row kernel: stages, stage size, CTAs per SM) are chosen by an
+// autotuner that times each candidate on the batch itself; timing writes
+// only the members' spare buffers, so it changes no state.
 #include <algorithm>
 #include <cstring>
 #include <string>
@@ -28,6 +39,8 @@
 
 #include "imexlbm.h"
 #include "imexlbm_internal.hpp"
+#include "bulk.cuh"
+#include "eng_lowp.cuh"
 #include "lattice_internal.hpp"
 #include "lowp_math.cuh"
 
@@ -48,6 +61,8 @@ struct BatchEntry {
     float eps;      // 2 - omega
     int sr;         // float16 storage: stochastic rounding
     uint32_t seed;  // stochastic-rounding seed at the start of the tick
+    int B;          // row kernel: y-rows per work item
+    unsigned ibegin;  // row kernel: packed index of the member's first item
     int pad;
 };
 
@@ -56,6 +71,16 @@ struct BatchHeader {
     int count;
     int pad;
 };
+
+// Table header of the row kernel's members.
+struct RowsHeader {
+    unsigned total;        // work items of all its members
+    int count;             // its members
+    unsigned stage_bytes;  // ring stage size (the largest member item)
+    int pad;
+};
+
+constexpr int kBatchRowThreads = 256;
 
 template <int P>
 __device__ __forceinline__ void batch_cell(const BatchEntry& e, unsigned long long local, int s, const CollideF32& base)
@@ -81,14 +106,11 @@ __device__ __forceinline__ void batch_cell(const BatchEntry& e, unsigned long lo
     for (int a = 0; a < kQ; ++a) h[a] = S::load(src + pi.at_dyn(g, a), a);
     CollideF32 cp = base;
     cp.eps = e.eps;
-    lowp::collide_dev_f32(h, cp);
+    lowp::collide_dev_f32<P>(h, cp);
     if constexpr (P == IMEX_F16DEV) {
-        if (e.sr) {
-            const uint32_t ch = lowp::sr_hash(local, e.seed + (uint32_t)s);
-#pragma unroll
-            for (int a = 0; a < kQ; ++a) h[a] = S::round_sr(h[a], lowp::sr_bits(ch, a));
-        }
-        lowp::store_f16_cell(h, [&](int a) -> T& { return dst[(size_t)a * e.plane + local]; });
+        auto at = [&](int a) -> T& { return dst[(size_t)a * e.plane + local]; };
+        if (e.sr) lowp::store_f16_cell_sr(h, lowp::sr_hash(local, e.seed + (uint32_t)s), at);
+        else lowp::store_f16_cell(h, at);
         return;
     }
 #pragma unroll
@@ -126,11 +148,150 @@ __global__ void __launch_bounds__(256) k_batch(const BatchHeader* __restrict__ h
     }
 }
 
+// Row-staged batched step (see the file header and rows.cuh).  One CTA per
+// slot of the persistent grid walks items blockIdx.x, + gridDim.x, ...
+__global__ void __launch_bounds__(kBatchRowThreads, 1)
+    k_batch_rows(const RowsHeader* __restrict__ hdr, const BatchEntry* __restrict__ tab, int s, CollideF32 base,
+                 int stages, unsigned* __restrict__ err)
+{
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ unsigned sbegin[kBatchMax + 1];
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem_raw);
+    unsigned char* ring = smem_raw + kRowBarrierBytes;
+    const int count = hdr->count;
+    const unsigned total = hdr->total;
+    const unsigned stage_bytes = hdr->stage_bytes;
+    for (int q = threadIdx.x; q < count; q += blockDim.x) sbegin[q] = tab[q].ibegin;
+    if (threadIdx.x == 0) sbegin[count] = total;
+    __syncthreads();
+    const unsigned G = gridDim.x;
+    const int my = blockIdx.x < total ? (int)((total - 1 - blockIdx.x) / G) + 1 : 0;
+    const int nwarps = blockDim.x >> 5;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int my_dir = warp + nwarps * lane;
+    const bool issuer = lane * nwarps < kQ && my_dir < kQ;
+
+    struct Item {
+        int m, x, y0;
+        bool active;
+    };
+    auto item_of = [&](int t) {
+        const unsigned it = blockIdx.x + (unsigned)t * G;
+        int lo = 0, hi = count;  // largest lo with sbegin[lo] <= it
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (sbegin[mid] <= it) lo = mid;
+            else hi = mid;
+        }
+        const BatchEntry& e = tab[lo];
+        const unsigned local = it - sbegin[lo];
+        const unsigned yblocks = (unsigned)(e.ny / e.B);
+        Item r;
+        r.m = lo;
+        r.x = (int)(local / yblocks);
+        r.y0 = (int)(local - (unsigned)r.x * yblocks) * e.B;
+        r.active = s < e.steps;
+        return r;
+    };
+    auto esize = [](int prec) { return prec == IMEX_F32 ? 4u : 2u; };
+    auto arm = [&](int t) {
+        const Item r = item_of(t);
+        const BatchEntry& e = tab[r.m];
+        const uint32_t bytes = r.active ? (uint32_t)kQ * e.B * e.nz * esize(e.prec) : 0u;
+        bulk::mbar_arrive_expect_tx(&full[t % stages], bytes);
+    };
+    auto issue = [&](int t) {
+        if (!issuer) return;
+        const Item r = item_of(t);
+        if (!r.active) return;
+        const BatchEntry& e = tab[r.m];
+        const uint32_t es = esize(e.prec);
+        const int B = e.B, nz = e.nz, ny = e.ny;
+        const uint32_t row_bytes = (uint32_t)nz * es;
+        const int a = my_dir;
+        int xs = r.x - ex(a, 0);
+        xs = xs < 0 ? xs + e.nx : xs >= e.nx ? xs - e.nx : xs;
+        const unsigned char* src = static_cast<const unsigned char*>(e.buf[e.cur ^ (s & 1)]);
+        const unsigned char* plane = src + ((size_t)a * e.plane + (size_t)xs * ny * nz) * es;
+        unsigned char* st = ring + (size_t)(t % stages) * stage_bytes + (size_t)a * B * row_bytes;
+        uint64_t* bar = &full[t % stages];
+        const int lo = r.y0 - ex(a, 1);
+        if (lo < 0) {
+            bulk::copy_g2s(st, plane + (size_t)(ny - 1) * row_bytes, row_bytes, bar);
+            if (B > 1) bulk::copy_g2s(st + row_bytes, plane, (uint32_t)(B - 1) * row_bytes, bar);
+        } else if (lo + B > ny) {
+            if (B > 1) bulk::copy_g2s(st, plane + (size_t)lo * row_bytes, (uint32_t)(B - 1) * row_bytes, bar);
+            bulk::copy_g2s(st + (size_t)(B - 1) * row_bytes, plane, row_bytes, bar);
+        } else {
+            bulk::copy_g2s(st, plane + (size_t)lo * row_bytes, (uint32_t)B * row_bytes, bar);
+        }
+    };
+
+    if (threadIdx.x == 0) {
+        for (int q = 0; q < stages; ++q) bulk::mbar_init(&full[q], 1);
+        bulk::fence_mbar_init();
+        for (int t = 0; t < stages && t < my; ++t) arm(t);
+    }
+    __syncthreads();
+    for (int t = 0; t < stages - 1 && t < my; ++t) issue(t);
+
+    for (int t = 0; t < my; ++t) {
+        if (t + stages - 1 < my) issue(t + stages - 1);
+        const int st_i = t % stages;
+        const int ok = bulk::mbar_wait(&full[st_i], (uint32_t)((t / stages) & 1));
+        if (__syncthreads_or(!ok)) {
+            if (threadIdx.x == 0) {
+                atomicOr(err, 1u);
+                const int last = t + stages - 1 < my ? t + stages - 1 : my - 1;
+                for (int q = t; q <= last; ++q) bulk::mbar_wait(&full[q % stages], (uint32_t)((q / stages) & 1));
+            }
+            __syncthreads();
+            return;
+        }
+        const Item r = item_of(t);
+        if (r.active) {
+            const BatchEntry& e = tab[r.m];
+            CollideF32 cp = base;
+            cp.eps = e.eps;
+            cp.sr = e.sr;
+            cp.seed = e.seed + (uint32_t)s;
+            const unsigned char* stg = ring + (size_t)st_i * stage_bytes;
+            void* dst = e.buf[e.cur ^ (s & 1) ^ 1];
+            const int nz = e.nz, n = e.B * nz, astride = e.B * nz;
+            const size_t row0 = ((size_t)r.x * e.ny + r.y0) * nz;  // first cell of the item
+            if (e.prec == IMEX_F32) {
+                const EngLowp<IMEX_F32> eng{cp};
+                for (int q = threadIdx.x; q < n; q += blockDim.x) {
+                    const int b = q / nz, z = q - b * nz;
+                    eng.run(reinterpret_cast<const float*>(stg) + (size_t)b * nz, astride, nz, z,
+                            static_cast<float*>(dst), e.plane, row0 + (size_t)b * nz);
+                }
+            } else {
+                const EngLowp<IMEX_F16DEV> eng{cp};
+                for (int q = threadIdx.x; q < n; q += blockDim.x) {
+                    const int b = q / nz, z = q - b * nz;
+                    eng.run(reinterpret_cast<const __half*>(stg) + (size_t)b * nz, astride, nz, z,
+                            static_cast<__half*>(dst), e.plane, row0 + (size_t)b * nz);
+                }
+            }
+        }
+        if (threadIdx.x == 0 && t + stages < my) arm(t + stages);
+        __syncthreads();
+    }
+}
+
 }  // namespace
 
 }  // namespace imex
 
 using namespace imex;
+
+// Row-kernel launch shape: ring depth, stage size and resident CTAs per SM
+// (stages 0: not chosen yet; -1: row kernel off, every member in the cell
+// kernel).
+struct RowShape {
+    int stages = 0, stage_kb = 0, ctas_per_sm = 0;
+};
 
 struct BatchShape {
     int threads = 0, cpt = 0, ctas_per_sm = 0;  // 0: not chosen yet
@@ -141,19 +302,27 @@ struct imex_batch {
     std::vector<int64_t> limit;  // total reference steps after which a member stops (-1: none)
     cudaStream_t stream = nullptr;
     cudaEvent_t done = nullptr;
-    BatchHeader* d_hdr = nullptr;
+    BatchHeader* d_hdr = nullptr;  // cell kernel's members
     BatchEntry* d_tab = nullptr;
     BatchHeader* h_hdr = nullptr;  // pinned staging
     BatchEntry* h_tab = nullptr;
+    RowsHeader* d_rhdr = nullptr;  // row kernel's members
+    BatchEntry* d_rtab = nullptr;
+    RowsHeader* h_rhdr = nullptr;
+    BatchEntry* h_rtab = nullptr;
+    unsigned* d_err = nullptr;  // set by the row kernel when a bounded wait runs out
     int capacity = 0;
     int device = 0;
     int sms = 0;
     BatchShape shape;
-    bool shape_pinned = false;
+    RowShape rshape;
+    int n_cell = 0, n_row = 0;  // members in each kernel (last uploaded table)
     int graph_steps = 0;  // K of the captured graph (0: no graph)
     cudaGraphExec_t graph = nullptr;
     int graph_k = 0;
     BatchShape graph_shape;
+    RowShape graph_rshape;
+    int graph_kinds = 0;  // bit 0: cell kernel, bit 1: row kernel
     int64_t launches = 0;
     std::string err;
 };
@@ -184,17 +353,37 @@ CollideF32 base_constants()
     return make_collide_f32(0.0);
 }
 
-cudaError_t launch_batch(imex_batch* b, const BatchShape& sh, int s)
+// Dynamic shared memory the row kernel may use (227 KB per CTA less its
+// static member table).
+constexpr int kRowsDynMax = 227 * 1024 - (int)sizeof(unsigned) * (kBatchMax + 1) - 1024;
+
+int kinds(const imex_batch* b) { return (b->n_cell > 0 ? 1 : 0) | (b->n_row > 0 ? 2 : 0); }
+
+// One step (index s of the tick) of every member: the cell kernel over its
+// members, then the row kernel over its members.
+cudaError_t launch_step(imex_batch* b, const BatchShape& sh, const RowShape& rs, int s)
 {
     const CollideF32 base = base_constants();
-    const dim3 grid((unsigned)(b->sms * sh.ctas_per_sm));
-    switch (sh.cpt) {
-    case 1: k_batch<1><<<grid, sh.threads, 0, b->stream>>>(b->d_hdr, b->d_tab, s, base); break;
-    case 2: k_batch<2><<<grid, sh.threads, 0, b->stream>>>(b->d_hdr, b->d_tab, s, base); break;
-    case 4: k_batch<4><<<grid, sh.threads, 0, b->stream>>>(b->d_hdr, b->d_tab, s, base); break;
-    default: return cudaErrorInvalidValue;
+    if (b->n_cell > 0) {
+        const dim3 grid((unsigned)(b->sms * sh.ctas_per_sm));
+        switch (sh.cpt) {
+        case 1: k_batch<1><<<grid, sh.threads, 0, b->stream>>>(b->d_hdr, b->d_tab, s, base); break;
+        case 2: k_batch<2><<<grid, sh.threads, 0, b->stream>>>(b->d_hdr, b->d_tab, s, base); break;
+        case 4: k_batch<4><<<grid, sh.threads, 0, b->stream>>>(b->d_hdr, b->d_tab, s, base); break;
+        default: return cudaErrorInvalidValue;
+        }
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
     }
-    return cudaGetLastError();
+    if (b->n_row > 0) {
+        const unsigned items = b->h_rhdr->total;
+        unsigned grid = (unsigned)(b->sms * rs.ctas_per_sm);
+        if (grid > items) grid = items;
+        const size_t smem = kRowBarrierBytes + (size_t)rs.stages * b->h_rhdr->stage_bytes;
+        k_batch_rows<<<grid, kBatchRowThreads, smem, b->stream>>>(b->d_rhdr, b->d_rtab, s, base, rs.stages, b->d_err);
+        return cudaGetLastError();
+    }
+    return cudaSuccess;
 }
 
 // Steps a member still owes before its limit.
@@ -205,16 +394,32 @@ int64_t owed(const imex_batch* b, size_t m, int64_t want)
     return left < 0 ? 0 : (left < want ? left : want);
 }
 
-// Write the member table for a tick where member m runs steps[m] fused
-// steps, and upload it (stream-ordered).
-int upload_table(imex_batch* b, const std::vector<int>& steps)
+// Rows per work item of a member in the row kernel under shape rs: the
+// largest divisor B of ny whose item (27 runs of B rows) fits a stage; 0 if
+// the member stays in the cell kernel.
+int rows_per_item(const imex_lattice* h, const RowShape& rs)
+{
+    if (rs.stages <= 0) return 0;
+    const size_t row_bytes = (size_t)h->g.nz * lattice_elem_size(h->precision);
+    const size_t cap = (size_t)rs.stage_kb * 1024;
+    if (row_bytes % 16 || (size_t)kQ * row_bytes > cap) return 0;
+    if ((size_t)h->g.nx * h->g.ny >= 0x7fffffffu) return 0;
+    for (int B = (int)std::min<size_t>((size_t)h->g.ny, cap / ((size_t)kQ * row_bytes)); B > 1; --B)
+        if (h->g.ny % B == 0) return B;
+    return 1;
+}
+
+// Write the member tables for a tick where member m runs steps[m] fused
+// steps under row shape rs, and upload them (stream-ordered).
+int upload_table(imex_batch* b, const std::vector<int>& steps, const RowShape& rs)
 {
     unsigned long long begin = 0;
-    int n = 0;
+    unsigned ibegin = 0, stage_bytes = 0;
+    int n = 0, nr = 0;
     for (size_t m = 0; m < b->members.size(); ++m) {
         imex_lattice* h = b->members[m];
-        BatchEntry& e = b->h_tab[n++];
-        e.begin = begin;
+        const int B = rows_per_item(h, rs);
+        BatchEntry& e = B ? b->h_rtab[nr++] : b->h_tab[n++];
         e.plane = h->ncells;
         e.buf[0] = h->buf[0];
         e.buf[1] = h->buf[1];
@@ -227,14 +432,34 @@ int upload_table(imex_batch* b, const std::vector<int>& steps)
         e.eps = h->cf32.eps;
         e.sr = h->cf32.sr;
         e.seed = (uint32_t)h->steps;
+        e.B = B;
         e.pad = 0;
-        begin += h->ncells;
+        if (B) {
+            e.begin = 0;
+            e.ibegin = ibegin;
+            ibegin += (unsigned)((size_t)h->g.nx * (h->g.ny / B));
+            stage_bytes = std::max(stage_bytes, (unsigned)(kQ * B * h->g.nz * lattice_elem_size(h->precision)));
+        } else {
+            e.begin = begin;
+            e.ibegin = 0;
+            begin += h->ncells;
+        }
     }
     b->h_hdr->total = begin;
     b->h_hdr->count = n;
+    b->h_rhdr->total = ibegin;
+    b->h_rhdr->count = nr;
+    b->h_rhdr->stage_bytes = stage_bytes;
+    b->n_cell = n;
+    b->n_row = nr;
     B_CUDA(b, cudaMemcpyAsync(b->d_tab, b->h_tab, sizeof(BatchEntry) * (n ? n : 1), cudaMemcpyHostToDevice, b->stream),
            "cudaMemcpyAsync");
     B_CUDA(b, cudaMemcpyAsync(b->d_hdr, b->h_hdr, sizeof(BatchHeader), cudaMemcpyHostToDevice, b->stream),
+           "cudaMemcpyAsync");
+    B_CUDA(b, cudaMemcpyAsync(b->d_rtab, b->h_rtab, sizeof(BatchEntry) * (nr ? nr : 1), cudaMemcpyHostToDevice,
+                              b->stream),
+           "cudaMemcpyAsync");
+    B_CUDA(b, cudaMemcpyAsync(b->d_rhdr, b->h_rhdr, sizeof(RowsHeader), cudaMemcpyHostToDevice, b->stream),
            "cudaMemcpyAsync");
     // the pinned staging is reused next tick: wait until the copies are done
     B_CUDA(b, cudaStreamSynchronize(b->stream), "cudaStreamSynchronize");
@@ -278,44 +503,90 @@ std::vector<BatchShape> candidates()
     return out;
 }
 
-// Time each candidate shape on the batch (step 0 of a one-step tick reads
-// buf[cur] and writes the other buffer, leaving every member's state as it
-// was) and keep the fastest.
-int tune_batch(imex_batch* b)
+// Row-kernel shapes: (stages, stage KB) per resident-CTA count, within the
+// shared memory of an SM.
+std::vector<RowShape> row_candidates()
+{
+    const int shapes[][3] = {{1, 2, 32}, {1, 3, 32}, {1, 4, 32}, {1, 2, 64}, {1, 3, 64}, {1, 2, 100},
+                             {2, 2, 24}, {2, 3, 24}, {2, 4, 24}, {2, 2, 48}, {3, 2, 16}, {3, 3, 16}};
+    std::vector<RowShape> out;
+    for (const auto& x : shapes) {
+        RowShape r;
+        r.ctas_per_sm = x[0];
+        r.stages = x[1];
+        r.stage_kb = x[2];
+        out.push_back(r);
+    }
+    return out;
+}
+
+// Milliseconds per step of shapes (sh, rs) on the current members: step 0
+// of a one-step tick reads buf[cur] and writes the other buffer, leaving
+// every member's state as it was.
+int time_step(imex_batch* b, const BatchShape& sh, const RowShape& rs, float* ms)
 {
     std::vector<int> one(b->members.size(), 1);
-    int rc = upload_table(b, one);
+    int rc = upload_table(b, one, rs);
     if (rc) return rc;
     cudaEvent_t e0, e1;
     B_CUDA(b, cudaEventCreate(&e0), "cudaEventCreate");
     B_CUDA(b, cudaEventCreate(&e1), "cudaEventCreate");
-    float best = 0.f;
-    BatchShape best_shape;
-    cudaError_t e = cudaSuccess;
-    for (const BatchShape& sh : candidates()) {
-        e = launch_batch(b, sh, 0);  // warm-up
-        for (int r = 0; r < 2 && e == cudaSuccess; ++r) e = launch_batch(b, sh, 0);
-        if (e == cudaSuccess) e = cudaEventRecord(e0, b->stream);
-        for (int r = 0; r < 3 && e == cudaSuccess; ++r) e = launch_batch(b, sh, 0);
-        if (e == cudaSuccess) e = cudaEventRecord(e1, b->stream);
-        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
-        float ms = 0.f;
-        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
-        if (e != cudaSuccess) break;
-        b->launches += 6;
-        if (!best_shape.threads || ms < best) {
-            best = ms;
-            best_shape = sh;
-        }
-    }
+    cudaError_t e = launch_step(b, sh, rs, 0);  // warm-up
+    for (int r = 0; r < 2 && e == cudaSuccess; ++r) e = launch_step(b, sh, rs, 0);
+    if (e == cudaSuccess) e = cudaEventRecord(e0, b->stream);
+    for (int r = 0; r < 3 && e == cudaSuccess; ++r) e = launch_step(b, sh, rs, 0);
+    if (e == cudaSuccess) e = cudaEventRecord(e1, b->stream);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    float t = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&t, e0, e1);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (e != cudaSuccess) return bcuda(b, e, "batch autotune");
-    b->shape = best_shape;
+    b->launches += 6 * ((b->n_cell > 0) + (b->n_row > 0));
+    *ms = t / 3;
     return IMEX_OK;
 }
 
-// Capture K launches (s = 0..K-1) of the current shape into a graph.
+// Pick the launch shapes: the cell kernel's shape with every member in it,
+// then each row-kernel shape (members that suit it move to the row kernel,
+// the rest stay in the cell kernel), keeping the fastest step.  Shapes set
+// by imex_batch_set_launch / imex_batch_set_row_launch are kept.
+int tune_batch(imex_batch* b, bool tune_cells, bool tune_rows)
+{
+    const RowShape off{-1, 0, 0};
+    float best = 0.f;
+    if (tune_cells) {
+        BatchShape best_shape;
+        for (const BatchShape& sh : candidates()) {
+            float ms = 0.f;
+            int rc = time_step(b, sh, off, &ms);
+            if (rc) return rc;
+            if (!best_shape.threads || ms < best) {
+                best = ms;
+                best_shape = sh;
+            }
+        }
+        b->shape = best_shape;
+    }
+    if (tune_rows) {
+        int rc = time_step(b, b->shape, off, &best);
+        if (rc) return rc;
+        RowShape best_rs = off;
+        for (const RowShape& rs : row_candidates()) {
+            float ms = 0.f;
+            rc = time_step(b, b->shape, rs, &ms);
+            if (rc) return rc;
+            if (b->n_row > 0 && ms < best) {
+                best = ms;
+                best_rs = rs;
+            }
+        }
+        b->rshape = best_rs;
+    }
+    return IMEX_OK;
+}
+
+// Capture K steps (s = 0..K-1) of the current shapes into a graph.
 int capture_graph(imex_batch* b, int K)
 {
     if (b->graph) {
@@ -325,7 +596,7 @@ int capture_graph(imex_batch* b, int K)
     cudaGraph_t g = nullptr;
     B_CUDA(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
     cudaError_t e = cudaSuccess;
-    for (int s = 0; s < K && e == cudaSuccess; ++s) e = launch_batch(b, b->shape, s);
+    for (int s = 0; s < K && e == cudaSuccess; ++s) e = launch_step(b, b->shape, b->rshape, s);
     cudaError_t e2 = cudaStreamEndCapture(b->stream, &g);
     if (e == cudaSuccess) e = e2;
     if (e == cudaSuccess) e = cudaGraphInstantiate(&b->graph, g, 0);
@@ -333,7 +604,17 @@ int capture_graph(imex_batch* b, int K)
     if (e != cudaSuccess) return bcuda(b, e, "batch graph capture");
     b->graph_k = K;
     b->graph_shape = b->shape;
+    b->graph_rshape = b->rshape;
+    b->graph_kinds = kinds(b);
     return IMEX_OK;
+}
+
+bool graph_valid(const imex_batch* b, int K)
+{
+    return b->graph && b->graph_k == K && b->graph_shape.threads == b->shape.threads &&
+           b->graph_shape.cpt == b->shape.cpt && b->graph_shape.ctas_per_sm == b->shape.ctas_per_sm &&
+           b->graph_rshape.stages == b->rshape.stages && b->graph_rshape.stage_kb == b->rshape.stage_kb &&
+           b->graph_rshape.ctas_per_sm == b->rshape.ctas_per_sm && b->graph_kinds == kinds(b);
 }
 
 }  // namespace
@@ -356,6 +637,14 @@ int imex_batch_create(int max_members, imex_batch** out)
     if (e == cudaSuccess) e = cudaMalloc(&b->d_tab, sizeof(BatchEntry) * max_members);
     if (e == cudaSuccess) e = cudaMallocHost(&b->h_hdr, sizeof(BatchHeader));
     if (e == cudaSuccess) e = cudaMallocHost(&b->h_tab, sizeof(BatchEntry) * max_members);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_rhdr, sizeof(RowsHeader));
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_rtab, sizeof(BatchEntry) * max_members);
+    if (e == cudaSuccess) e = cudaMallocHost(&b->h_rhdr, sizeof(RowsHeader));
+    if (e == cudaSuccess) e = cudaMallocHost(&b->h_rtab, sizeof(BatchEntry) * max_members);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_err, sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMemset(b->d_err, 0, sizeof(unsigned));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_batch_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, kRowsDynMax);
     if (e != cudaSuccess) {
         imex_batch_destroy(b);
         cudaGetLastError();
@@ -375,6 +664,11 @@ void imex_batch_destroy(imex_batch* b)
     if (b->d_tab) cudaFree(b->d_tab);
     if (b->h_hdr) cudaFreeHost(b->h_hdr);
     if (b->h_tab) cudaFreeHost(b->h_tab);
+    if (b->d_rhdr) cudaFree(b->d_rhdr);
+    if (b->d_rtab) cudaFree(b->d_rtab);
+    if (b->h_rhdr) cudaFreeHost(b->h_rhdr);
+    if (b->h_rtab) cudaFreeHost(b->h_rtab);
+    if (b->d_err) cudaFree(b->d_err);
     if (b->done) cudaEventDestroy(b->done);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
@@ -433,8 +727,8 @@ int imex_batch_step(imex_batch* b, int nsteps)
     }
     int rc = join_members(b);
     if (rc) return rc;
-    if (!b->shape.threads) {
-        rc = tune_batch(b);
+    if (!b->shape.threads || !b->rshape.stages) {
+        rc = tune_batch(b, !b->shape.threads, !b->rshape.stages);
         if (rc) return rc;
     }
     std::vector<int> tick(b->members.size());
@@ -445,19 +739,18 @@ int imex_batch_step(imex_batch* b, int nsteps)
         const int K = b->graph_steps > 0 ? b->graph_steps : 1;
         const int k = (int)std::min<int64_t>(most, K);
         for (size_t m = 0; m < left.size(); ++m) tick[m] = (int)std::min<int64_t>(left[m], k);
-        rc = upload_table(b, tick);
+        rc = upload_table(b, tick, b->rshape);
         if (rc) return rc;
         if (b->graph_steps > 0 && k == b->graph_steps) {
-            if (!b->graph || b->graph_k != k || b->graph_shape.threads != b->shape.threads ||
-                b->graph_shape.cpt != b->shape.cpt || b->graph_shape.ctas_per_sm != b->shape.ctas_per_sm) {
+            if (!graph_valid(b, k)) {
                 rc = capture_graph(b, k);
                 if (rc) return rc;
             }
             B_CUDA(b, cudaGraphLaunch(b->graph, b->stream), "cudaGraphLaunch");
         } else {
-            for (int s = 0; s < k; ++s) B_CUDA(b, launch_batch(b, b->shape, s), "batch kernel launch");
+            for (int s = 0; s < k; ++s) B_CUDA(b, launch_step(b, b->shape, b->rshape, s), "batch kernel launch");
         }
-        b->launches += k;
+        b->launches += (int64_t)k * ((b->n_cell > 0) + (b->n_row > 0));
         for (size_t m = 0; m < left.size(); ++m) {
             imex_lattice* h = b->members[m];
             h->cur ^= tick[m] & 1;
@@ -472,7 +765,14 @@ int imex_batch_step(imex_batch* b, int nsteps)
 int imex_batch_synchronize(imex_batch* b)
 {
     if (!b) return set_thread_error(IMEX_ERR_ARG, "imex_batch_synchronize: null batch");
+    unsigned v = 0;
+    B_CUDA(b, cudaMemcpyAsync(&v, b->d_err, sizeof v, cudaMemcpyDeviceToHost, b->stream), "cudaMemcpyAsync");
     B_CUDA(b, cudaStreamSynchronize(b->stream), "imex_batch_synchronize");
+    if (v) {
+        B_CUDA(b, cudaMemset(b->d_err, 0, sizeof v), "cudaMemset");
+        return bfail(b, IMEX_ERR_CUDA, "imex_batch_synchronize: a row kernel's asynchronous copy did not complete in "
+                                       "time; the members' results are invalid");
+    }
     return IMEX_OK;
 }
 
@@ -499,6 +799,32 @@ int imex_batch_get_launch(imex_batch* b, int out[3])
     out[0] = b->shape.threads;
     out[1] = b->shape.cpt;
     out[2] = b->shape.ctas_per_sm;
+    return IMEX_OK;
+}
+
+int imex_batch_set_row_launch(imex_batch* b, int stages, int stage_kb, int ctas_per_sm)
+{
+    if (!b) return set_thread_error(IMEX_ERR_ARG, "imex_batch_set_row_launch: null batch");
+    if (stages == 0 || stages == -1) {  // 0: autotune, -1: row kernel off
+        b->rshape = RowShape{stages, 0, 0};
+        return IMEX_OK;
+    }
+    if (stages < 2 || stages > 8 || stage_kb < 4 || ctas_per_sm < 1 || ctas_per_sm > 4 ||
+        (size_t)stages * stage_kb * 1024 + kRowBarrierBytes > (size_t)kRowsDynMax ||
+        ctas_per_sm * ((size_t)stages * stage_kb * 1024 + kRowBarrierBytes + sizeof(unsigned) * (kBatchMax + 1) + 1024) >
+            228 * 1024)
+        return bfail(b, IMEX_ERR_ARG, "imex_batch_set_row_launch: 2 <= stages <= 8, stage_kb >= 4, 1 <= ctas_per_sm "
+                                      "<= 4, and the CTAs' rings must fit an SM's shared memory");
+    b->rshape = RowShape{stages, stage_kb, ctas_per_sm};
+    return IMEX_OK;
+}
+
+int imex_batch_get_row_launch(imex_batch* b, int out[3])
+{
+    if (!b || !out) return set_thread_error(IMEX_ERR_ARG, "imex_batch_get_row_launch: null argument");
+    out[0] = b->rshape.stages;
+    out[1] = b->rshape.stage_kb;
+    out[2] = b->rshape.ctas_per_sm;
     return IMEX_OK;
 }
 

@@ -69,6 +69,12 @@ void LBM::fence() { check(imex_synchronize(h_)); }
 
 void LBM::ComputeMacroscopic(double* p, double* u, double* v, double* w) { check(imex_macroscopic(h_, p, u, v, w)); }
 
+void LBM::MPIoutput(int n) { check(imex_write_tecplot(h_, nullptr, n)); }
+
+void LBM::profile_enable(bool on) { check(imex_profile_enable(h_, on ? 1 : 0)); }
+
+void LBM::profile_read(imex_phase_stats out[IMEX_NPHASE], bool reset) { check(imex_profile_read(h_, out, reset ? 1 : 0)); }
+
 void LBM::Conserved(double& mass, double& mom_x, double& mom_y, double& mom_z, double& ke)
 {
     // A diverged run (NaN/Inf) still reports its values, as the reference

@@ -68,7 +68,11 @@ struct LBM {
     void Streaming();
     void ComputeMacroscopic(double* p, double* u, double* v, double* w);
     void Conserved(double& mass, double& mom_x, double& mom_y, double& mom_z, double& ke);
+    void MPIoutput(int n);  // lbm.cpp:307-598: writes output<n>.plt
     void fence();
+    // per-phase device time of this lattice's kernels (imex_profile_*)
+    void profile_enable(bool on);
+    void profile_read(imex_phase_stats out[IMEX_NPHASE], bool reset);
 
     imex_lattice* handle() const { return h_; }
 

@@ -1,5 +1,5 @@
 // Reduced-precision storage kernels: float32 distributions (IMEX_F32) and
-// float16 deviations f - w (IMEX_F16DEV), collided in float32 by
+// float16 deviations 2^12 (f - w) (IMEX_F16DEV), collided in float32 by
 // lowp::collide_dev_f32 (lowp_math.cuh, which explains the arithmetic);
 // diagnostics accumulate in float64.
 #include <cmath>
@@ -8,6 +8,7 @@
 
 #include "kernels_lowp.cuh"
 #include "lowp_math.cuh"
+#include "eng_lowp.cuh"
 #include "rows.cuh"
 #include "tg_init.cuh"
 
@@ -42,48 +43,16 @@ __global__ void __launch_bounds__(kStepBlock) k_step_lowp(const typename Storage
 #pragma unroll
         for (int a = 0; a < kQ; ++a) h[a] = S::load_plain(src + (size_t)a * g.plane + cell, a);
     }
-    collide_dev_f32(h, cp);
+    collide_dev_f32<P>(h, cp);
     if constexpr (P == IMEX_F16DEV) {
-        if (cp.sr) {
-            const uint32_t ch = lowp::sr_hash(cell, cp.seed);
-#pragma unroll
-            for (int a = 0; a < kQ; ++a) h[a] = S::round_sr(h[a], lowp::sr_bits(ch, a));
-        }
-        lowp::store_f16_cell(h, [&](int a) -> __half& { return dst[(size_t)a * g.plane + cell]; });
+        auto at = [&](int a) -> __half& { return dst[(size_t)a * g.plane + cell]; };
+        if (cp.sr) lowp::store_f16_cell_sr(h, lowp::sr_hash(cell, cp.seed), at);
+        else lowp::store_f16_cell(h, at);
         return;
     }
 #pragma unroll
     for (int a = 0; a < kQ; ++a) dst[(size_t)a * g.plane + cell] = S::store(h[a], a);
 }
-
-// Row-kernel engine: float32 collision of one staged cell.
-template <int P>
-struct EngLowp {
-    using T = typename Storage<P>::T;
-    static constexpr int kMinBlocks = 4;
-    CollideF32 cp;
-
-    __device__ __forceinline__ void run(const T* __restrict__ st, int astride, int nz, int z, T* __restrict__ dst,
-                                        size_t plane, size_t rowoff) const
-    {
-        const int zm = z == 0 ? nz - 1 : z - 1, zp = z == nz - 1 ? 0 : z + 1;
-        float h[kQ];
-#pragma unroll
-        for (int a = 0; a < kQ; ++a) h[a] = Storage<P>::load_plain(st + a * astride + pull_z(ex(a, 2), z, zm, zp), a);
-        collide_dev_f32(h, cp);
-        if constexpr (P == IMEX_F16DEV) {
-            if (cp.sr) {
-                const uint32_t ch = lowp::sr_hash(rowoff + z, cp.seed);
-#pragma unroll
-                for (int a = 0; a < kQ; ++a) h[a] = Storage<P>::round_sr(h[a], lowp::sr_bits(ch, a));
-            }
-            lowp::store_f16_cell(h, [&](int a) -> T& { return dst[(size_t)a * plane + rowoff + z]; });
-            return;
-        }
-#pragma unroll
-        for (int a = 0; a < kQ; ++a) dst[(size_t)a * plane + rowoff + z] = Storage<P>::store(h[a], a);
-    }
-};
 
 // Taylor-Green initial state (float64 equilibrium, src/lbm.cpp:78-108),
 // rounded once into the storage format.

@@ -255,6 +255,7 @@ int launch_mode(imex_lattice* h, int mode)
         if (rc) return rc;
     }
     h->cf32.seed = (uint32_t)h->steps;  // stochastic rounding: a new stream of bits every step
+    PhaseScope timed(h->prof, mode == kModeStream ? IMEX_PHASE_STREAM : IMEX_PHASE_COLLISION, h->stream);
     if (mode == kModeFused && h->rows.stages > 0)
         e = launch_fused_rows(h, src, dst, h->rows);
     else if (lowp(h))
@@ -346,33 +347,47 @@ int imex_create(int nx, int ny, int nz, double tau, double rho0, double u0, int 
 
     const size_t arr = (size_t)kQ * h->ncells * elem_size(precision);
     const size_t nparts = conserved_partials(h->g);
-    const size_t need = 2 * arr + nparts * 5 * sizeof(double) + 64;
+    // scratch: conserved partials, 5 reduced values, fallback counter, error flag
+    const size_t scratch = nparts * 5 * sizeof(double) + 5 * sizeof(double) + 2 * sizeof(unsigned long long);
+    const size_t need = 2 * arr + scratch;
+    // Device memory comes from the device's stream-ordered pool: creating
+    // and destroying lattices (a server does it per request) then neither
+    // synchronises the device nor returns memory to the driver.  Memory the
+    // pool holds but no lattice uses counts as free.
+    cudaMemPool_t pool = nullptr;
+    e = cudaDeviceGetDefaultMemPool(&pool, h->device);
     size_t free_b = 0, total_b = 0;
-    e = cudaMemGetInfo(&free_b, &total_b);
+    if (e == cudaSuccess) e = cudaMemGetInfo(&free_b, &total_b);
     if (e != cudaSuccess) return bail(cuda_fail(nullptr, e, "cudaMemGetInfo"));
-    if (need > free_b) {
+    unsigned long long reserved = 0, used = 0;
+    cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemCurrent, &reserved);
+    cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, &used);
+    const size_t avail = free_b + (reserved > used ? (size_t)(reserved - used) : 0);
+    if (need > avail) {
         char msg[160];
         std::snprintf(msg, sizeof msg, "imex_create: needs %.3f GB of device memory, %.3f GB free", need / 1e9,
-                      free_b / 1e9);
+                      avail / 1e9);
         return bail(set_thread_error(IMEX_ERR_MEMORY, msg));
     }
-    for (int b = 0; b < 2; ++b) {
-        e = cudaMalloc(&h->buf[b], arr);
-        if (e != cudaSuccess) return bail(set_thread_error(IMEX_ERR_MEMORY, "imex_create: cudaMalloc of f failed"));
-    }
-    e = cudaMalloc(&h->d_partial, nparts * 5 * sizeof(double));
-    if (e == cudaSuccess) e = cudaMalloc(&h->d_out, 5 * sizeof(double));
-    if (e == cudaSuccess) e = cudaMalloc(&h->d_fallback, sizeof(unsigned long long));
-    if (e == cudaSuccess) e = cudaMalloc(&h->d_err, sizeof(unsigned));
-    if (e == cudaSuccess) e = cudaMallocHost(&h->h_out, 5 * sizeof(double));
-    if (e != cudaSuccess) return bail(set_thread_error(IMEX_ERR_MEMORY, "imex_create: scratch allocation failed"));
     e = cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) return bail(cuda_fail(nullptr, e, "cudaStreamCreate"));
     h->stream = h->own_stream;
-    e = cudaMemsetAsync(h->d_fallback, 0, sizeof(unsigned long long), h->stream);
-    if (e == cudaSuccess) e = cudaMemsetAsync(h->d_err, 0, sizeof(unsigned), h->stream);
-    if (e != cudaSuccess) return bail(cuda_fail(nullptr, e, "cudaMemset"));
-    h->bytes = 2 * arr + nparts * 5 * sizeof(double) + 5 * sizeof(double) + sizeof(unsigned long long);
+    for (int b = 0; b < 2 && e == cudaSuccess; ++b) e = cudaMallocAsync(&h->buf[b], arr, h->stream);
+    unsigned char* s = nullptr;
+    if (e == cudaSuccess) e = cudaMallocAsync((void**)&s, scratch, h->stream);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return bail(set_thread_error(IMEX_ERR_MEMORY, "imex_create: device allocation failed"));
+    }
+    h->scratch = s;
+    h->d_partial = reinterpret_cast<double*>(s);
+    h->d_out = h->d_partial + nparts * 5;
+    h->d_fallback = reinterpret_cast<unsigned long long*>(h->d_out + 5);
+    h->d_err = reinterpret_cast<unsigned*>(h->d_fallback + 1);
+    e = cudaMemsetAsync(h->d_fallback, 0, 2 * sizeof(unsigned long long), h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);  // usable from any stream from here on
+    if (e != cudaSuccess) return bail(cuda_fail(nullptr, e, "imex_create"));
+    h->bytes = need;
     *out = h;
     return IMEX_OK;
 }
@@ -381,15 +396,21 @@ void imex_destroy(imex_lattice* h)
 {
     if (!h) return;
     cudaSetDevice(h->device);
-    if (h->stream) cudaStreamSynchronize(h->stream);
-    for (void* p : h->buf)
-        if (p) cudaFree(p);
-    if (h->d_partial) cudaFree(h->d_partial);
-    if (h->d_out) cudaFree(h->d_out);
-    if (h->d_fallback) cudaFree(h->d_fallback);
-    if (h->d_err) cudaFree(h->d_err);
-    if (h->h_out) cudaFreeHost(h->h_out);
-    if (h->own_stream) cudaStreamDestroy(h->own_stream);
+    if (h->own_stream) {
+        // release after the handle's queued work, on whichever stream it is
+        if (h->stream && h->stream != h->own_stream) {
+            cudaEvent_t ev;
+            if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) == cudaSuccess) {
+                cudaEventRecord(ev, h->stream);
+                cudaStreamWaitEvent(h->own_stream, ev, 0);
+                cudaEventDestroy(ev);
+            }
+        }
+        for (void* p : h->buf)
+            if (p) cudaFreeAsync(p, h->own_stream);
+        if (h->scratch) cudaFreeAsync(h->scratch, h->own_stream);
+        cudaStreamDestroy(h->own_stream);
+    }
     delete h;
 }
 
@@ -406,8 +427,8 @@ int imex_initialize_phase(imex_lattice* h, double phx, double phy, double phz)
     //   x = (double)(i - ghost + x_lo) / (double)glx * 2.0 * pi, pi = 3.1415926
     const int n[3] = {h->g.nx, h->g.ny, h->g.nz};
     const size_t tot = 3 * ((size_t)n[0] + n[1] + n[2]);
-    double* host = nullptr;
-    IMEX_CUDA(h, cudaMallocHost(&host, tot * sizeof(double)), "cudaMallocHost");
+    std::vector<double> table(tot);
+    double* host = table.data();
     size_t off = 0;
     size_t offs[3];
     for (int d = 0; d < 3; ++d) {
@@ -432,7 +453,6 @@ int imex_initialize_phase(imex_lattice* h, double phx, double phy, double phz)
         e = cudaFreeAsync(dev, h->stream);
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
-    cudaFreeHost(host);
     if (e != cudaSuccess) return cuda_fail(h, e, "imex_initialize");
     h->cur = 0;
     h->tag = kExact;
@@ -482,19 +502,22 @@ int imex_conserved(imex_lattice* h, double out[5])
     if (rc) return rc;
     if (!out) return fail(h, IMEX_ERR_ARG, "imex_conserved: null output");
     const bool pull = h->tag == kPendingStream;
+    int timed = h->prof.start(IMEX_PHASE_CONSERVED, h->stream);
     cudaError_t e =
         lowp(h) ? launch_conserved_lowp(h->precision, pull, h->buf[h->cur], h->g, h->d_partial, h->d_out, h->stream)
         : use_fixed(h) ? launch_conserved_fx(pull, dbuf(h, h->cur), h->g, h->fx, h->d_partial, h->d_out, h->stream)
                        : launch_conserved_f64(pull, dbuf(h, h->cur), h->g, h->d_partial, h->d_out, h->stream);
+    h->prof.stop(timed, h->stream);
     if (e != cudaSuccess) return cuda_fail(h, e, "conserved kernel launch");
     h->launches += 2;
-    IMEX_CUDA(h, cudaMemcpyAsync(h->h_out, h->d_out, 5 * sizeof(double), cudaMemcpyDeviceToHost, h->stream), "cudaMemcpy");
+    double res[5];
+    IMEX_CUDA(h, cudaMemcpyAsync(res, h->d_out, 5 * sizeof(double), cudaMemcpyDeviceToHost, h->stream), "cudaMemcpy");
     IMEX_CUDA(h, cudaStreamSynchronize(h->stream), "imex_conserved");
     rc = check_kernel_error(h);
     if (rc) return rc;
     bool finite = true;
     for (int q = 0; q < 5; ++q) {
-        out[q] = h->h_out[q];
+        out[q] = res[q];
         finite = finite && std::isfinite(out[q]);
     }
     if (!finite) return fail(h, IMEX_ERR_NONFINITE, "imex_conserved: non-finite diagnostics (the run diverged)");
@@ -510,6 +533,7 @@ namespace {
 int macro_fields(imex_lattice* h, double* p, double* u, double* v, double* w)
 {
     const bool pull = h->tag == kPendingStream;
+    PhaseScope timed(h->prof, IMEX_PHASE_MACRO, h->stream);
     cudaError_t e = lowp(h) ? launch_macro_lowp(h->precision, pull, h->buf[h->cur], h->g, p, u, v, w, h->stream)
                             : launch_macro_f64(pull, dbuf(h, h->cur), h->g, p, u, v, w, h->stream);
     if (e != cudaSuccess) return cuda_fail(h, e, "macroscopic kernel launch");
@@ -669,6 +693,22 @@ int imex_set_stream(imex_lattice* h, void* s)
 {
     if (!h) return set_thread_error(IMEX_ERR_ARG, "imex_set_stream: null handle");
     h->stream = s ? static_cast<cudaStream_t>(s) : h->own_stream;
+    return IMEX_OK;
+}
+
+int imex_profile_enable(imex_lattice* h, int on)
+{
+    if (!h) return set_thread_error(IMEX_ERR_ARG, "imex_profile_enable: null handle");
+    IMEX_CUDA(h, cudaSetDevice(h->device), "cudaSetDevice");
+    h->prof.enable(on != 0);
+    return IMEX_OK;
+}
+
+int imex_profile_read(imex_lattice* h, imex_phase_stats out[IMEX_NPHASE], int reset)
+{
+    if (!h || !out) return set_thread_error(IMEX_ERR_ARG, "imex_profile_read: null argument");
+    IMEX_CUDA(h, cudaSetDevice(h->device), "cudaSetDevice");
+    h->prof.read(out, reset != 0);
     return IMEX_OK;
 }
 

@@ -10,6 +10,7 @@
 #include "kernels_f64.cuh"
 #include "kernels_fx.cuh"
 #include "kernels_lowp.cuh"
+#include "phase_timer.hpp"
 #include "rows.cuh"
 
 using imex::CollideF32;
@@ -36,9 +37,9 @@ struct imex_lattice {
     cudaStream_t own_stream = nullptr;
     cudaStream_t stream = nullptr;
     int device = 0;
+    unsigned char* scratch = nullptr;  // one allocation holding the four below
     double* d_partial = nullptr;  // conserved partials (5 per block)
     double* d_out = nullptr;      // 5 reduced values
-    double* h_out = nullptr;      // pinned copy of d_out
     unsigned long long* d_fallback = nullptr;  // fixed-point engine fallback counter
     size_t bytes = 0;
     CollideF64 cf64{};
@@ -49,6 +50,7 @@ struct imex_lattice {
     RowConfig rows{};           // launch shape of the fused step (stages 0: one thread per cell)
     int shape_mode = -1;        // -1 autotune on first use, 0 one thread per cell, 1 row-staged
     bool shape_pinned = false;  // shape set by imex_set_launch rather than the autotuner
+    imex::PhaseTimer prof;      // per-phase device time (imex_profile_*)
     std::string err;
 };
 

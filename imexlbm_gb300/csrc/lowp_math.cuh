@@ -1,5 +1,5 @@
 // Reduced-precision storage: float32 distributions (IMEX_F32) and float16
-// deviations from the lattice weights, h = f - w (IMEX_F16DEV).  Both
+// deviations from the lattice weights, 2^12 (f - w) (IMEX_F16DEV).  Both
 // collide in float32; diagnostics accumulate in float64.
 //
 // The float32 collision works in deviation space for both formats: with
@@ -53,12 +53,12 @@ __device__ __forceinline__ uint32_t sr_hash(unsigned long long idx, uint32_t see
     return x;
 }
 
-// Random bits for direction a of a cell: the Weyl sequence r0 + a * phi
-// (mod 2^32, phi = 2^32 / golden ratio) from the cell's hash r0.  Each value
-// is uniform because r0 is; across the 27 directions the draws are
-// stratified rather than independent, which if anything lowers the
-// variance of the cell's summed rounding error.
-__device__ __forceinline__ uint32_t sr_bits(uint32_t cell_hash, int a) { return cell_hash + (uint32_t)a * 0x9E3779B9u; }
+// Random word k of a cell: the Weyl sequence r0 + k * phi (mod 2^32, phi =
+// 2^32 / golden ratio) from the cell's hash r0.  Each word is uniform
+// because r0 is; across a cell's words the draws are stratified rather
+// than independent, which if anything lowers the variance of the cell's
+// summed rounding error.
+__device__ __forceinline__ uint32_t sr_bits(uint32_t cell_hash, int k) { return cell_hash + (uint32_t)k * 0x9E3779B9u; }
 
 // Store 27 float16 deviations of one cell, converting two at a time
 // (values already on the float16 grid convert exactly).
@@ -74,9 +74,49 @@ __device__ __forceinline__ void store_f16_cell(const float (&y)[kQ], Dst&& at)
     at(kQ - 1) = __float2half_rn(y[kQ - 1]);
 }
 
+// Stochastic rounding of a float32 pair to float16 in one instruction
+// (cvt.rs.f16x2.f32 of the sm_100 family).  Each value moves to one of its
+// two float16 neighbours, up (in magnitude) with probability equal to its
+// distance from the lower one in units of their gap, resolved to 13 bits:
+// the value's dropped bits plus 13 random bits, carried into the kept part.
+// `hi` (upper half of the result) takes random bits 16..28 of `rbits`, `lo`
+// bits 0..12.  A normal float16 result (|x| >= 2^-14) drops exactly 13 bits,
+// so the expected stored value is x exactly; for subnormal results the
+// probability is truncated to a multiple of 2^-13, a bias toward zero below
+// 2^-37 per value.
+__device__ __forceinline__ uint32_t cvt_rs_f16x2(float hi, float lo, uint32_t rbits)
+{
+    uint32_t d;
+    asm("cvt.rs.f16x2.f32 %0, %1, %2, %3;" : "=r"(d) : "f"(hi), "f"(lo), "r"(rbits));
+    return d;
+}
+
+// Store 27 float16 deviations of one cell with stochastic rounding: pair
+// (a, a + 1) draws the 32-bit word sr_bits(cell_hash, a / 2).
+template <class Dst>
+__device__ __forceinline__ void store_f16_cell_sr(const float (&y)[kQ], uint32_t cell_hash, Dst&& at)
+{
+#pragma unroll
+    for (int a = 0; a + 1 < kQ; a += 2) {
+        const uint32_t d = cvt_rs_f16x2(y[a + 1], y[a], sr_bits(cell_hash, a >> 1));
+        at(a) = __ushort_as_half((unsigned short)(d & 0xffffu));
+        at(a + 1) = __ushort_as_half((unsigned short)(d >> 16));
+    }
+    const uint32_t d = cvt_rs_f16x2(0.0f, y[kQ - 1], sr_bits(cell_hash, kQ >> 1));
+    at(kQ - 1) = __ushort_as_half((unsigned short)(d & 0xffffu));
+}
+
+// kScale: the collision works on kScale * (f - w).  float32 storage keeps f
+// itself (kScale 1); float16 storage keeps (f - w) * 2^12, so that
+// deviations down to 2^-26 (rather than 2^-14) are normal float16 numbers
+// with the full 11-bit significand - deviations of populations whose e.u is
+// near zero are of order w u^2, below 2^-14 at u ~ 0.01.  The largest
+// storable deviation, 65504 / 2^12 = 16, is far above any f - w of a
+// physical state (|f - w| < 1).
 template <>
 struct Storage<IMEX_F32> {
     using T = float;
+    static constexpr float kScale = 1.0f;
     static __device__ __forceinline__ float load(const float* p, int a)
     {
         return __ldg(p) - (float)weight(a);
@@ -90,33 +130,30 @@ struct Storage<IMEX_F32> {
 template <>
 struct Storage<IMEX_F16DEV> {
     using T = __half;
+    static constexpr float kScale = 4096.0f;
     static __device__ __forceinline__ float load(const __half* p, int) { return __half2float(__ldg(p)); }
     static __device__ __forceinline__ float load_plain(const __half* p, int) { return __half2float(*p); }
     static __device__ __forceinline__ __half store(float h, int) { return __float2half_rn(h); }
-    static __device__ __forceinline__ double to_f64(__half v, int a) { return weight(a) + (double)__half2float(v); }
-    // Stochastic rounding to float16, as float32 bits: h moved up or down to
-    // a neighbouring float16 value with probabilities that make the expected
-    // result exactly h.  `bits` is a uniform 32-bit random number.  Adding
-    // `drop` random bits below the float16 precision of |h| and clearing
-    // them rounds the magnitude up with probability (dropped part) / 2^drop;
-    // a carry into the exponent lands on the next float16 value, the correct
-    // upper neighbour.  drop = 13 in the normal float16 range (|h| >= 2^-14)
-    // and one more per binade below (float16 subnormals are 2^-24 apart),
-    // up to the 23 float32 mantissa bits.  The result is exactly
-    // representable in float16, so any rounding conversion stores it as is.
-    static __device__ __forceinline__ float round_sr(float h, uint32_t bits)
+    static __device__ __forceinline__ double to_f64(__half v, int a)
     {
-        const uint32_t x = __float_as_uint(h);
-        const int e = (int)((x >> 23) & 0xffu);
-        const uint32_t mask = (1u << min(max(126 - e, 13), 23)) - 1u;
-        return __uint_as_float((x + (bits & mask)) & ~mask);  // |h| < 65504: no carry into the sign
+        return weight(a) + (double)__half2float(v) * (1.0 / kScale);
     }
-    static __device__ __forceinline__ __half from_f64(double f, int a) { return __float2half_rn((float)(f - weight(a))); }
+    static __device__ __forceinline__ __half from_f64(double f, int a)
+    {
+        return __float2half_rn((float)((f - weight(a)) * kScale));
+    }
 };
 
-// float32 BGK collision of the deviations h (see the file header).
+// float32 BGK collision of the deviations h = kScale (f - w) (see the file
+// header).  Moments and the relaxation are linear in h; only the quadratic
+// terms of the equilibrium carry 1 / kScale, folded into their constants.
+// kScale is a power of two, so every intermediate is exactly kScale^k times
+// the unscaled one and the result is exactly kScale times the unscaled
+// collision's: both storage formats run the same float32 arithmetic.
+template <int P>
 __device__ __forceinline__ void collide_dev_f32(float (&h)[kQ], const CollideF32& cp)
 {
+    constexpr float c15 = -1.5f / Storage<P>::kScale, c45 = 4.5f / Storage<P>::kScale;
     float d[kPairs + 1], s[kPairs + 1];
 #pragma unroll
     for (int k = 1; k <= kPairs; ++k) {
@@ -135,7 +172,7 @@ __device__ __forceinline__ void collide_dev_f32(float (&h)[kQ], const CollideF32
             if (e == -1) u[dim] -= d[k];
         }
     const float udu = fmaf(u[2], u[2], fmaf(u[1], u[1], u[0] * u[0]));
-    const float base = fmaf(-1.5f, udu, sig);
+    const float base = fmaf(c15, udu, sig);
     const float eps = cp.eps;
     {
         const float heq = cp.w[0] * base;
@@ -155,7 +192,7 @@ __device__ __forceinline__ void collide_dev_f32(float (&h)[kQ], const CollideF32
                 first = false;
             }
         }
-        const float A = cp.w[cls] * fmaf(4.5f * edu, edu, base);
+        const float A = cp.w[cls] * fmaf(c45 * edu, edu, base);
         const float B = cp.w3[cls] * edu;
         const float ep = A + B, em = A - B;
         h[a] = fmaf(eps, h[a] - ep, fmaf(2.f, ep, -h[a]));

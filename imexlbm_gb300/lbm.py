@@ -127,6 +127,36 @@ class LBM:
         self._check(self._L.imex_velocity_max_diff(self._h, ref._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
         return float(out[0]), float(out[1])
 
+    def profile_enable(self, on: bool = True) -> None:
+        self._check(self._L.imex_profile_enable(self._h, int(bool(on))))
+
+    def profile_read(self, reset: bool = False) -> dict:
+        """{phase: {calls, total_ms, min_ms, max_ms}} of the timed launches."""
+        buf = (_lib.PhaseStats * _lib.IMEX_NPHASE)()
+        self._check(self._L.imex_profile_read(self._h, buf, int(bool(reset))))
+        names = ("collision", "stream", "macro", "conserved")
+        return {names[q]: {k: getattr(buf[q], k) for k, _ in _lib.PhaseStats._fields_} for q in range(_lib.IMEX_NPHASE)}
+
+    def minmax_uvwp(self):
+        """(umax, vmax, wmax, pmax, umin, vmin, wmin, pmin), the reducer
+        order of the reference's "minmax_uvwp" (src/lbm.cpp:351-372)."""
+        out = np.zeros(8)
+        self._check(self._L.imex_minmax_uvwp(self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+        return tuple(float(x) for x in out)
+
+    def MPIoutput(self, n: int, path: str | None = None) -> str:
+        """Write the reference's Tecplot file output<n>.plt (src/lbm.cpp:307)
+        or ``path``; returns the file name."""
+        name = path if path is not None else f"output{int(n)}.plt"
+        self._check(self._L.imex_write_tecplot(self._h, name.encode(), int(n)))
+        return name
+
+    def checkpoint_save(self, path: str) -> None:
+        self._check(self._L.imex_checkpoint_save(self._h, str(path).encode()))
+
+    def checkpoint_load(self, path: str) -> None:
+        self._check(self._L.imex_checkpoint_load(self._h, str(path).encode()))
+
     # -- data access --------------------------------------------------------
     def get_f(self, out: np.ndarray | None = None) -> np.ndarray:
         f = np.empty(self.shape) if out is None else out
@@ -224,6 +254,15 @@ class Batch:
         self._check(self._L.imex_batch_get_launch(self._b, out))
         return tuple(out)
 
+    def set_row_launch(self, stages: int, stage_kb: int = 32, ctas_per_sm: int = 1) -> None:
+        """Row-staged kernel shape; stages 0 autotunes, -1 turns it off."""
+        self._check(self._L.imex_batch_set_row_launch(self._b, int(stages), int(stage_kb), int(ctas_per_sm)))
+
+    def get_row_launch(self):
+        out = (ctypes.c_int * 3)()
+        self._check(self._L.imex_batch_get_row_launch(self._b, out))
+        return tuple(out)
+
     def set_graph(self, steps: int) -> None:
         self._check(self._L.imex_batch_set_graph(self._b, int(steps)))
 
@@ -248,4 +287,68 @@ class Batch:
         self.close()
 
 
-__all__ = ["System", "LBM", "Batch", "ImexError", "Q"]
+class Server:
+    """Request server with continuous batching (include/imexlbm.h,
+    imex_server_*): submit solves from any thread, poll finished results."""
+
+    def __init__(self, budget_bytes: float = 120e9, max_active: int = 256, steps_per_tick: int = 25):
+        self._L = _lib.load()
+        s = ctypes.c_void_p()
+        check(self._L.imex_server_create(int(budget_bytes), int(max_active), int(steps_per_tick), ctypes.byref(s)))
+        self._s = s
+
+    def submit(self, nx: int, ny: int, nz: int, tau: float, u0: float, steps: int, precision: int = _lib.IMEX_F32,
+               rho0: float = 1.0, phase=(0.0, 0.0, 0.0), rounding: int | None = None, tag: int = 0) -> int:
+        r = _lib.Request()
+        r.nx, r.ny, r.nz = int(nx), int(ny), int(nz)
+        r.precision = int(precision)
+        if rounding is None:
+            rounding = _lib.IMEX_ROUND_STOCHASTIC if precision == _lib.IMEX_F16DEV else _lib.IMEX_ROUND_NEAREST
+        r.rounding = int(rounding)
+        r.tau, r.rho0, r.u0 = float(tau), float(rho0), float(u0)
+        for i in range(3):
+            r.phase[i] = float(phase[i])
+        r.steps, r.tag = int(steps), int(tag)
+        rid = ctypes.c_int64()
+        check(self._L.imex_server_submit(self._s, ctypes.byref(r), ctypes.byref(rid)))
+        return int(rid.value)
+
+    def poll(self, max_results: int = 4096):
+        buf = (_lib.Result * max_results)()
+        n = ctypes.c_int()
+        check(self._L.imex_server_poll(self._s, buf, max_results, ctypes.byref(n)))
+        out = []
+        for i in range(n.value):
+            r = buf[i]
+            out.append({"id": r.id, "tag": r.tag, "status": r.status, "conserved": tuple(r.conserved),
+                        "steps": r.steps, "cells": r.cells, "t_submit": r.t_submit, "t_admit": r.t_admit,
+                        "t_done": r.t_done})
+        return out
+
+    def stats(self) -> dict:
+        st = _lib.ServerStats()
+        check(self._L.imex_server_get_stats(self._s, ctypes.byref(st)))
+        return {name: getattr(st, name) for name, _ in _lib.ServerStats._fields_}
+
+    def now(self) -> float:
+        return float(self._L.imex_server_now(self._s))
+
+    def close(self) -> None:
+        if getattr(self, "_s", None):
+            self._L.imex_server_destroy(self._s)
+            self._s = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+__all__ = ["System", "LBM", "Batch", "Server", "ImexError", "Q"]

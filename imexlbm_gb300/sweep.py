@@ -5,7 +5,7 @@ Default workload: 512^3, Re = 1600, u0 = 0.05, 2000 steps, reporting every
 100 - three runs side by side:
   (a) float64 storage (the reference's precision; fixed-point engine),
   (b) float32 storage, float32 collision,
-  (c) float16 storage of f - w, float32 collision, rounded to nearest,
+  (c) float16 storage of 2^12 (f - w), float32 collision, rounded to nearest,
   (d) the same with stochastic rounding.
 Every report step prints, for (b) and (c) against (a): the relative
 kinetic-energy error, the largest velocity difference over all cells (in

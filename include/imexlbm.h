@@ -34,16 +34,17 @@ extern "C" {
 #define IMEX_ERR_DECK 4      /* input deck missing or malformed                     */
 #define IMEX_ERR_NONFINITE 5 /* diagnostics produced NaN or Inf                     */
 #define IMEX_ERR_STATE 6     /* call out of sequence (e.g. step before initialize)  */
+#define IMEX_ERR_IO 7        /* a file could not be opened, read or written         */
 
 /* Storage precision of the distributions. */
 #define IMEX_F64 0    /* float64 storage (the reference's own precision)        */
 #define IMEX_F32 1    /* float32 storage, float32 collision                     */
-#define IMEX_F16DEV 2 /* float16 storage of f_a - w_a, float32 collision        */
+#define IMEX_F16DEV 2 /* float16 storage of (f_a - w_a) * 2^12, float32 collision */
 
 /* Rounding of float16-deviation storage (imex_set_rounding). */
 #define IMEX_ROUND_NEAREST 0    /* round to nearest even                               */
-#define IMEX_ROUND_STOCHASTIC 1 /* round up or down with probabilities that keep the
-                                   expected stored value exact                          */
+#define IMEX_ROUND_STOCHASTIC 1 /* round up or down with probabilities (13-bit) that
+                                   keep the expected stored value exact                 */
 
 /* Arithmetic engine of the float64 collision. */
 #define IMEX_ENGINE_AUTO 0   /* fastest engine that meets float64 parity            */
@@ -126,6 +127,54 @@ int imex_macroscopic(imex_lattice *h, double *p, double *u, double *v, double *w
  * Compares a reduced-precision run against a float64 run without moving
  * the fields to the host.  Synchronises both handles' streams. */
 int imex_velocity_max_diff(imex_lattice *a, imex_lattice *b, double out[2]);
+
+/* Per-phase device time of a lattice's kernels, for the per-phase profile
+ * report of the reference's profiling build (src/profile.hpp:53-70,
+ * src/profile.cpp:107-200).  While enabled, each kernel launch of the phase
+ * is bracketed by CUDA events on the handle's stream - no synchronisation
+ * is added to the step - and its device time is folded into calls, total,
+ * min and max when the statistics are read.  Phases: */
+#define IMEX_PHASE_COLLISION 0 /* fused step / collision kernels (P_COLLISION)   */
+#define IMEX_PHASE_STREAM 1    /* streaming applied alone (P_STREAM_*)           */
+#define IMEX_PHASE_MACRO 2     /* macroscopic fields, min/max, output (P_MACRO)  */
+#define IMEX_PHASE_CONSERVED 3 /* conserved-quantity reduction                   */
+#define IMEX_NPHASE 4
+typedef struct imex_phase_stats {
+    int64_t calls;
+    double total_ms, min_ms, max_ms;
+} imex_phase_stats;
+int imex_profile_enable(imex_lattice *h, int on);
+/* Read (and with reset != 0 clear) the statistics; waits for the timed
+ * launches to finish. */
+int imex_profile_read(imex_lattice *h, imex_phase_stats out[IMEX_NPHASE], int reset);
+
+/* Extremes of the macroscopic fields: out = {umax, vmax, wmax, pmax, umin,
+ * vmin, wmin, pmin} over all cells, with p = sum f / 3 and (u, v, w) =
+ * sum f e as ComputeMacroscopic forms them.  The "minmax_uvwp" reduction of
+ * LBM::MPIoutput (src/lbm.cpp:351-372), in its reducer order; NaN values
+ * are skipped and an all-NaN field gives -DBL_MAX / DBL_MAX, the
+ * reduction's identities.  One fused pass over f, no field arrays.
+ * Synchronises. */
+int imex_minmax_uvwp(imex_lattice *h, double out[8]);
+
+/* Write the binary Tecplot file of LBM::MPIoutput(n) (src/lbm.cpp:307-598)
+ * for this lattice: the 332-byte "#!TDV112" header with solution time n
+ * and the field ranges, then seven float64 blocks x, y, z, u, v, w, p in
+ * x-fastest order, node coordinates index / (extent - 1).  path NULL
+ * writes "output<n>.plt" in the working directory, the reference's name.
+ * Device staging: 32 bytes per cell for the duration of the call.
+ * Returns IMEX_ERR_IO if the file cannot be written.  Synchronises. */
+int imex_write_tecplot(imex_lattice *h, const char *path, int n);
+
+/* Save the lattice's state - stored distributions in their storage
+ * precision, the step count, whether a streaming is pending, the rounding
+ * mode - to a file, and load it back into a lattice of the same size and
+ * precision, which then continues bit for bit as the saved one would have
+ * (stochastic rounding included).  tau, rho0 and u0 stay the loading
+ * handle's own.  No reference counterpart: the reference has no restart
+ * file.  Not while the lattice is a batch member.  Both synchronise. */
+int imex_checkpoint_save(imex_lattice *h, const char *path);
+int imex_checkpoint_load(imex_lattice *h, const char *path);
 
 /* Copy the current distributions (reference order, float64) to the host
  * buffer of n = 27*nx*ny*nz values.  The reference exposes them as the
@@ -254,6 +303,17 @@ int imex_batch_synchronize(imex_batch *b);
 int imex_batch_set_launch(imex_batch *b, int threads, int cells_per_thread, int ctas_per_sm);
 int imex_batch_get_launch(imex_batch *b, int out[3]);
 
+/* Launch shape of the row-staged batch kernel, which takes the members
+ * whose z-rows are a multiple of 16 bytes (nz * element size): ring depth
+ * `stages`, stage size `stage_kb` KiB (a member's work item is the largest
+ * block of y-rows whose 27 source runs fit one stage) and resident CTAs
+ * per SM.  stages 0 autotunes (default); -1 turns the row kernel off, so
+ * every member runs in the cell kernel.  imex_batch_get_row_launch gives
+ * {stages, stage_kb, ctas_per_sm} (-1 when the tuner found the cell
+ * kernel faster). */
+int imex_batch_set_row_launch(imex_batch *b, int stages, int stage_kb, int ctas_per_sm);
+int imex_batch_get_row_launch(imex_batch *b, int out[3]);
+
 /* Steps per captured CUDA graph (default 16; 0 launches each step
  * directly). */
 int imex_batch_set_graph(imex_batch *b, int steps_per_graph);
@@ -261,6 +321,68 @@ int imex_batch_set_graph(imex_batch *b, int steps_per_graph);
 /* Kernel launches issued by the batch (one per batched step). */
 int64_t imex_batch_kernel_launches(const imex_batch *b);
 const char *imex_batch_last_error(const imex_batch *b);
+
+/* --------------------------------------------------------------- server -- */
+
+/* A request server with continuous batching (no counterpart in the
+ * reference).  Callers submit Taylor-Green solves from any thread; a server
+ * thread admits them in arrival order while a slot is free and their device
+ * memory fits the budget, advances all admitted requests together in one
+ * batched launch per step (CUDA graphs of steps_per_tick steps), and retires
+ * each at its step count, between ticks, publishing its diagnostics.  New
+ * requests join while others run; every result is bit-identical to running
+ * the request alone. */
+typedef struct imex_server imex_server;
+
+typedef struct imex_request {
+    int nx, ny, nz;       /* lattice size */
+    int precision;        /* IMEX_F32 or IMEX_F16DEV */
+    int rounding;         /* IMEX_ROUND_* (IMEX_F16DEV storage) */
+    int pad;
+    double tau, rho0, u0; /* as imex_create */
+    double phase[3];      /* as imex_initialize_phase */
+    int64_t steps;        /* reference steps to run */
+    int64_t tag;          /* caller's tag, returned in the result */
+} imex_request;
+
+typedef struct imex_result {
+    int64_t id, tag;
+    int status;           /* IMEX_OK, or the error that stopped the request */
+    int pad;
+    double conserved[5];  /* mass, px, py, pz, ke after `steps` (imex_conserved) */
+    int64_t steps;        /* steps run */
+    int64_t cells;
+    double t_submit, t_admit, t_done; /* seconds on the server clock */
+} imex_result;
+
+typedef struct imex_server_stats {
+    int64_t queued, active, completed, bytes_in_use;
+    int64_t cell_updates; /* lattice-cell updates done by the batch */
+    int64_t ticks;
+    double busy_seconds;  /* wall time inside ticks */
+    double now;           /* server clock */
+    int64_t failed;       /* 1 if the server thread stopped on an error */
+} imex_server_stats;
+
+/* Start a server on the current device with a device-memory budget for the
+ * admitted requests' distributions, at most max_active (<= 2048) requests
+ * in flight, and steps_per_tick steps per batched tick. */
+int imex_server_create(size_t budget_bytes, int max_active, int steps_per_tick, imex_server **out);
+
+/* Queue a request (thread-safe); *id identifies its result. */
+int imex_server_submit(imex_server *s, const imex_request *req, int64_t *id);
+
+/* Move up to max finished results into out (thread-safe, non-blocking);
+ * *n receives how many. */
+int imex_server_poll(imex_server *s, imex_result *out, int max, int *n);
+
+int imex_server_get_stats(imex_server *s, imex_server_stats *out);
+
+/* Seconds since the server started (the clock of the results' times). */
+double imex_server_now(const imex_server *s);
+
+/* Stop the server thread; requests still queued or running are dropped. */
+void imex_server_destroy(imex_server *s);
 
 /* Library version string. */
 const char *imex_version(void);

@@ -12,6 +12,8 @@
  *   fused BGK collision       src/lbm.cpp:131-166
  *   pull streaming            src/lbm.cpp:168-207
  *   conserved diagnostics     src/lbm.cpp:266-306
+ *   min/max of u, v, w, p     src/lbm.cpp:351-372
+ *   Tecplot output (1 rank)   src/lbm.cpp:307-598
  * On one rank the reference's ghost-layer halo (src/mpi_view_transfer.cpp:
  * 260-456: faces, then edges, then corners, all self-channels) makes every
  * ghost cell a periodic image of an interior cell, so streaming here reads
@@ -329,4 +331,112 @@ void oracle_macroscopic(int nx, int ny, int nz, const double *f,
         v[c] = vl;
         w[c] = wl;
     }
+}
+
+/* Extremes of u, v, w, p, the "minmax_uvwp" reduction of src/lbm.cpp:351-372:
+ * out = {umax, vmax, wmax, pmax, umin, vmin, wmin, pmin}, each reducer
+ * starting from Kokkos's Max / Min identity (-DBL_MAX / DBL_MAX) and updated
+ * by a strict comparison, so NaN values are never taken. */
+void oracle_minmax_uvwp(int nx, int ny, int nz, const double *f, double out[8])
+{
+    const size_t n = (size_t)nx * ny * nz;
+    double *m = (double *)malloc(4 * n * sizeof(double));
+    oracle_macroscopic(nx, ny, nz, f, m + 3 * n, m, m + n, m + 2 * n); /* u v w p */
+    for (int c = 0; c < 4; ++c)
+    {
+        double mx = -1.7976931348623157e308, mn = 1.7976931348623157e308;
+        for (size_t q = 0; q < n; ++q)
+        {
+            const double x = m[c * n + q];
+            if (x > mx) mx = x;
+            if (x < mn) mn = x;
+        }
+        out[c] = mx;
+        out[4 + c] = mn;
+    }
+    free(m);
+}
+
+static void put_i32(FILE *fp, int v) { int32_t x = v; fwrite(&x, 4, 1, fp); }
+static void put_f32(FILE *fp, float v) { fwrite(&v, 4, 1, fp); }
+static void put_f64(FILE *fp, double v) { fwrite(&v, 8, 1, fp); }
+
+/* LBM::MPIoutput(n) on one rank (src/lbm.cpp:307-598): the header fields in
+ * the order the reference writes them (:397-562, 332 bytes), then the
+ * blocks x, y, z, u, v, w, p as the one-rank file view lays them out
+ * (:564-591: each block the whole lattice in Fortran order, x fastest).
+ * Coordinates are (double)i / (nx - 1) (:341-343).  Returns 0, or -1 if the
+ * file cannot be written. */
+int oracle_write_tecplot(int nx, int ny, int nz, const double *f, int n, const char *path)
+{
+    const size_t cells = (size_t)nx * ny * nz;
+    double mm[8];
+    oracle_minmax_uvwp(nx, ny, nz, f, mm);
+    double *m = (double *)malloc(4 * cells * sizeof(double));
+    oracle_macroscopic(nx, ny, nz, f, m + 3 * cells, m, m + cells, m + 2 * cells);
+    FILE *fp = fopen(path, "wb");
+    if (!fp)
+    {
+        free(m);
+        return -1;
+    }
+    fwrite("#!TDV112", 1, 8, fp);
+    put_i32(fp, 1);
+    put_i32(fp, 0);
+    put_i32(fp, 0);
+    put_i32(fp, 7);
+    const char *names = "xyzuvwp";
+    for (int c = 0; c < 7; ++c)
+    {
+        put_i32(fp, names[c]);
+        put_i32(fp, 0);
+    }
+    put_f32(fp, 299.0f);
+    const char *zone = "ZONE 001";
+    for (int c = 0; c < 8; ++c)
+        put_i32(fp, zone[c]);
+    put_i32(fp, 0);
+    put_i32(fp, -1);
+    put_f64(fp, (double)n);
+    put_i32(fp, 0);
+    put_i32(fp, -1);
+    for (int c = 0; c < 4; ++c)
+        put_i32(fp, 0);
+    put_i32(fp, nx);
+    put_i32(fp, ny);
+    put_i32(fp, nz);
+    put_i32(fp, 0);
+    put_f32(fp, 357.0f);
+    put_f32(fp, 299.0f);
+    for (int c = 0; c < 7; ++c)
+        put_i32(fp, 2);
+    put_i32(fp, 0);
+    put_i32(fp, 0);
+    put_i32(fp, -1);
+    for (int c = 0; c < 3; ++c)
+    {
+        put_f64(fp, 0.0);
+        put_f64(fp, 1.0);
+    }
+    for (int c = 0; c < 4; ++c)
+    {
+        put_f64(fp, mm[4 + c]);
+        put_f64(fp, mm[c]);
+    }
+    for (int b = 0; b < 7; ++b)
+        for (int k = 0; k < nz; ++k)
+            for (int j = 0; j < ny; ++j)
+                for (int i = 0; i < nx; ++i)
+                {
+                    double x;
+                    if (b == 0) x = (double)i / (nx - 1);
+                    else if (b == 1) x = (double)j / (ny - 1);
+                    else if (b == 2) x = (double)k / (nz - 1);
+                    else x = m[(size_t)(b - 3) * cells + ((size_t)i * ny + j) * nz + k];
+                    put_f64(fp, x);
+                }
+    const int bad = ferror(fp);
+    fclose(fp);
+    free(m);
+    return bad ? -1 : 0;
 }

@@ -62,6 +62,9 @@ def lib():
         L.oracle_step_pingpong.argtypes = [i, i, i, ctypes.c_double, dp, dp]
         L.oracle_conserved.argtypes = [i, i, i, dp, dp]
         L.oracle_macroscopic.argtypes = [i, i, i, dp, dp, dp, dp, dp]
+        L.oracle_minmax_uvwp.argtypes = [i, i, i, dp, dp]
+        L.oracle_write_tecplot.argtypes = [i, i, i, dp, i, ctypes.c_char_p]
+        L.oracle_write_tecplot.restype = i
         _lib = L
     return _lib
 
@@ -137,3 +140,18 @@ def macroscopic(f: np.ndarray):
     p, u, v, w = (np.empty((nx, ny, nz)) for _ in range(4))
     lib().oracle_macroscopic(nx, ny, nz, _p(f), _p(p), _p(u), _p(v), _p(w))
     return p, u, v, w
+
+
+def minmax_uvwp(f: np.ndarray) -> np.ndarray:
+    """(umax, vmax, wmax, pmax, umin, vmin, wmin, pmin) of f's macroscopic fields."""
+    _, nx, ny, nz = f.shape
+    out = np.zeros(8)
+    lib().oracle_minmax_uvwp(nx, ny, nz, _p(f), _p(out))
+    return out
+
+
+def write_tecplot(f: np.ndarray, n: int, path: str) -> None:
+    """The reference's one-rank output<n>.plt of f, written to path."""
+    _, nx, ny, nz = f.shape
+    if lib().oracle_write_tecplot(nx, ny, nz, _p(f), int(n), str(path).encode()) != 0:
+        raise OSError(f"cannot write {path}")

@@ -70,6 +70,61 @@ def test_batch_launch_shapes_and_graphs(imex, shape, graph):
         lat.close()
 
 
+ROW_SPECS = SPECS + [  # rows of a multiple of 16 bytes: the row-staged kernel takes these
+    ((24, 20, 48), "f16dev", 0.003, 0.05, (0.2, 0.4, 0.6)),
+    ((32, 32, 32), "f16dev", 0.001, 0.07, (1.5, 2.5, 0.5)),
+    ((16, 12, 64), "f32", 0.02, 0.04, (0.0, 1.0, 2.0)),
+    ((9, 7, 8), "f16dev", 0.05, 0.06, (0.3, 0.3, 0.3)),
+]
+
+
+@pytest.mark.parametrize("row_shape", [(-1, 0, 0), (2, 32, 1), (3, 16, 2), (4, 4, 1), (2, 100, 1)])
+@pytest.mark.parametrize("graph", [0, 6])
+def test_row_kernel_equals_alone(imex, row_shape, graph):
+    """The row-staged batch kernel (and the cell kernel beside it for the
+    members it does not take) ends every member where it would alone."""
+    steps = 13
+    want = [alone(imex, s, steps) for s in ROW_SPECS]
+    lats = [make(imex, s) for s in ROW_SPECS]
+    with imex.Batch(16) as b:
+        b.set_row_launch(*row_shape)
+        b.set_graph(graph)
+        for lat in lats:
+            b.add(lat)
+        b.step(steps)
+        assert b.get_row_launch() == tuple(row_shape)
+        for i, (lat, w) in enumerate(zip(lats, want)):
+            assert np.array_equal(lat.get_f(), w), i
+    for lat in lats:
+        lat.close()
+
+
+def test_row_kernel_member_limits(imex):
+    """Members stop mid-tick at their step limits inside the row kernel."""
+    specs = ROW_SPECS[6:]
+    limits = [3, 11, -1, 7]
+    lats = [make(imex, s) for s in specs]
+    with imex.Batch(8) as b:
+        b.set_row_launch(2, 32, 1)
+        b.set_graph(5)
+        for lat, lim in zip(lats, limits):
+            b.add(lat, lim)
+        b.step(12)
+    for lat, spec, lim in zip(lats, specs, limits):
+        n = 12 if lim < 0 else lim
+        assert lat.steps_done() == n
+        assert np.array_equal(lat.get_f(), alone(imex, spec, n))
+        lat.close()
+
+
+def test_row_launch_checks(imex):
+    with imex.Batch(2) as b:
+        with pytest.raises(imex.ImexError):
+            b.set_row_launch(2, 200, 2)       # two CTAs' rings exceed an SM
+        with pytest.raises(imex.ImexError):
+            b.set_row_launch(1, 32, 1)        # one stage cannot overlap
+
+
 def test_members_join_leave_and_finish(imex):
     """Continuous batching: members admitted and retired between steps, with
     per-member step limits, each ending where it would alone."""

@@ -101,3 +101,45 @@ def test_weights_and_velocities(oracle):
     assert np.allclose(np.einsum("a,ai,aj->ij", w, e, e), np.eye(3) / 3)
     opp = [0, 2, 1, 4, 3, 6, 5, 8, 7, 10, 9, 12, 11, 14, 13, 16, 15, 18, 17, 20, 19, 22, 21, 24, 23, 26, 25]
     assert np.array_equal(e[opp], -e)
+
+
+def test_minmax_uvwp(oracle):
+    f = oracle.init(9, 7, 5, 1.0, 0.05)
+    oracle.step(f, 0.01, 3)
+    p, u, v, w = oracle.macroscopic(f)
+    got = oracle.minmax_uvwp(f)
+    want = [u.max(), v.max(), w.max(), p.max(), u.min(), v.min(), w.min(), p.min()]
+    assert list(got) == want
+
+
+def test_tecplot_layout(oracle, tmp_path):
+    """The oracle's output<n>.plt follows the byte layout LBM::MPIoutput
+    writes (src/lbm.cpp:397-591): section ends at bytes 20, 80, 120, 172,
+    220 and 332 as the reference's own comments count them, then seven
+    x-fastest float64 blocks."""
+    import struct
+    nx, ny, nz = 6, 5, 4
+    f = oracle.init(nx, ny, nz, 1.0, 0.05)
+    path = tmp_path / "output7.plt"
+    oracle.write_tecplot(f, 7, str(path))
+    b = path.read_bytes()
+    n = nx * ny * nz
+    assert len(b) == 332 + 7 * n * 8
+    assert b[:8] == b"#!TDV112"
+    assert struct.unpack_from("<3i", b, 8) == (1, 0, 0)
+    assert struct.unpack_from("<15i", b, 20) == (7, 120, 0, 121, 0, 122, 0, 117, 0, 118, 0, 119, 0, 112, 0)
+    assert struct.unpack_from("<f9i", b, 80) == (299.0, 90, 79, 78, 69, 32, 48, 48, 49, 0)
+    assert struct.unpack_from("<i", b, 120)[0] == -1
+    assert struct.unpack_from("<d", b, 124)[0] == 7.0
+    assert struct.unpack_from("<10i", b, 132) == (0, -1, 0, 0, 0, 0, nx, ny, nz, 0)
+    assert struct.unpack_from("<ff7i3i", b, 172) == (357.0, 299.0, 2, 2, 2, 2, 2, 2, 2, 0, 0, -1)
+    rng = struct.unpack_from("<14d", b, 220)
+    mm = oracle.minmax_uvwp(f)
+    assert rng == (0.0, 1.0, 0.0, 1.0, 0.0, 1.0, mm[4], mm[0], mm[5], mm[1], mm[6], mm[2], mm[7], mm[3])
+    blocks = np.frombuffer(b, dtype="<f8", offset=332).reshape(7, nz, ny, nx)
+    i = np.arange(nx)
+    assert np.array_equal(blocks[0][2, 3], i / (nx - 1))
+    assert np.array_equal(blocks[2][:, 0, 0], np.arange(nz) / (nz - 1))
+    p, u, v, w = oracle.macroscopic(f)
+    for blk, fld in zip(blocks[3:], (u, v, w, p)):
+        assert np.array_equal(blk, fld.transpose(2, 1, 0))

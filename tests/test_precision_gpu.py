@@ -1,4 +1,4 @@
-"""Reduced-precision storage (float32 f, float16 f - w) against the float64
+"""Reduced-precision storage (float32 f, float16 (f - w) 2^12) against the float64
 oracle, through the C ABI.
 
 Tolerances come from the error these formats carry, not from parity:
@@ -29,7 +29,7 @@ def stored(oracle, prec, imex, f):
     if prec == imex.IMEX_F32:
         return f.astype(np.float32).astype(np.float64)
     w = weights(oracle)
-    return w + (f - w).astype(np.float16).astype(np.float64)
+    return w + ((f - w) * 4096.0).astype(np.float16).astype(np.float64) / 4096.0
 
 
 PRECS = [("f32", 2e-5, 1e-4, 1e-8), ("f16dev", 2e-4, 5e-3, 1e-6)]
@@ -134,6 +134,11 @@ def test_stochastic_rounding_is_deterministic_and_kernel_independent(imex):
     assert np.array_equal(runs[0], runs[1])
     assert np.array_equal(runs[0], runs[2])
     with imex.LBM(*shape, 0.002, 1.0, 0.05, precision=imex.IMEX_F16DEV) as lat:
+        lat.Initialize()
+        lat.step(21)
+        assert np.array_equal(lat.get_f(), runs[0])       # stochastic rounding is the default
+    with imex.LBM(*shape, 0.002, 1.0, 0.05, precision=imex.IMEX_F16DEV) as lat:
+        lat.set_rounding(imex.IMEX_ROUND_NEAREST)
         lat.Initialize()
         lat.step(21)
         assert not np.array_equal(lat.get_f(), runs[0])   # nearest rounding differs

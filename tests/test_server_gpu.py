@@ -1,0 +1,91 @@
+"""The continuous-batching request server.
+
+Requests are submitted while others run; each result must equal the same
+request run alone, bit for bit (same arithmetic, same stochastic-rounding
+bits), requests must join the batch while others are in flight, and bad
+requests must be refused at submission.
+"""
+import time
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+REQS = [  # edge, tau, u0, steps, precision name
+    (48, 0.004, 0.05, 600, "f32"),      # still running when the others arrive
+    (16, 0.004, 0.05, 37, "f32"),
+    (24, 0.02, 0.06, 25, "f16dev"),
+    (32, 0.0007, 0.04, 60, "f32"),
+    (16, 0.01, 0.07, 9, "f16dev"),
+    (8, 0.1, 0.03, 50, "f32"),
+    (20, 0.003, 0.05, 44, "f16dev"),
+    (12, 0.05, 0.05, 0, "f32"),
+    (28, 0.002, 0.08, 31, "f32"),
+]
+
+
+def prec(imex, name):
+    return {"f32": imex.IMEX_F32, "f16dev": imex.IMEX_F16DEV}[name]
+
+
+def alone(imex, r):
+    edge, tau, u0, steps, pname = r
+    with imex.LBM(edge, edge, edge, tau, 1.0, u0, precision=prec(imex, pname)) as lat:
+        lat.Initialize()
+        lat.step(steps)
+        return lat.Conserved()
+
+
+def test_results_equal_alone_and_requests_overlap(imex):
+    with imex.Server(budget_bytes=2e9, max_active=4, steps_per_tick=7) as srv:
+        for i, r in enumerate(REQS):
+            edge, tau, u0, steps, pname = r
+            srv.submit(edge, edge, edge, tau, u0, steps, prec(imex, pname), tag=i)
+            time.sleep(0.002)
+        got = {}
+        t0 = time.time()
+        while len(got) < len(REQS) and time.time() - t0 < 120:
+            for res in srv.poll():
+                got[res["tag"]] = res
+            time.sleep(0.01)
+        st = srv.stats()
+    assert len(got) == len(REQS) and st["failed"] == 0
+    for i, r in enumerate(REQS):
+        res = got[i]
+        assert res["status"] == 0, res
+        assert res["steps"] == r[3]
+        assert res["t_submit"] <= res["t_admit"] <= res["t_done"]
+        assert res["conserved"] == alone(imex, r), i
+    # continuous batching: requests were admitted while the first one ran,
+    # and finished before it
+    first = got[0]
+    joined = [i for i in got if i and first["t_admit"] < got[i]["t_admit"] < first["t_done"]]
+    assert joined and any(got[i]["t_done"] < first["t_done"] for i in joined)
+    assert st["completed"] == len(REQS) and st["cell_updates"] > 0
+
+
+def test_budget_and_slots_queue_requests(imex):
+    """With one slot, requests run one after another in arrival order."""
+    with imex.Server(budget_bytes=1e9, max_active=1, steps_per_tick=5) as srv:
+        for i in range(3):
+            srv.submit(16, 16, 16, 0.01, 0.05, 12, imex.IMEX_F32, tag=i)
+        got = []
+        t0 = time.time()
+        while len(got) < 3 and time.time() - t0 < 60:
+            got += srv.poll()
+            time.sleep(0.01)
+    got.sort(key=lambda r: r["tag"])
+    assert [r["status"] for r in got] == [0, 0, 0]
+    for a, b in zip(got, got[1:]):
+        assert b["t_admit"] >= a["t_done"] - 1e-6
+
+
+def test_bad_requests_refused(imex):
+    with imex.Server(budget_bytes=1e8, max_active=2, steps_per_tick=5) as srv:
+        with pytest.raises(imex.ImexError):
+            srv.submit(8, 8, 8, 0.01, 0.05, 5, imex.IMEX_F64)      # float64 is not batched
+        with pytest.raises(imex.ImexError):
+            srv.submit(256, 256, 256, 0.01, 0.05, 5, imex.IMEX_F32)  # larger than the budget
+        with pytest.raises(imex.ImexError):
+            srv.submit(0, 8, 8, 0.01, 0.05, 5, imex.IMEX_F32)
