@@ -59,6 +59,8 @@ def parse_args(argv=None):
     ap.add_argument("--report-every", type=int, default=100)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--launch", default=None, metavar="STAGES,ROWS,CTAS",
+                    help="pin the fused step's launch shape instead of autotuning it (stages 0: one thread per cell)")
     return ap.parse_args(argv)
 
 
@@ -239,6 +241,8 @@ def run_ours(a):
     lat.set_stream(stream.cuda_stream)
     if a.precision == "f16dev":
         lat.set_rounding(m.IMEX_ROUND_STOCHASTIC if a.rounding == "stochastic" else m.IMEX_ROUND_NEAREST)
+    if a.launch:
+        lat.set_launch(*(int(v) for v in a.launch.split(",")))
     lat.Initialize()
     eng_name = "fixed" if (engine == m.IMEX_ENGINE_FIXED) else "native" if engine == m.IMEX_ENGINE_NATIVE else "auto"
     if prec != m.IMEX_F64:

@@ -132,7 +132,8 @@ SIGNATURES = {
     "imex_batch_synchronize": (ctypes.c_int, [ctypes.c_void_p]),
     "imex_batch_set_launch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     "imex_batch_get_launch": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]),
-    "imex_batch_set_row_launch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    "imex_batch_set_row_launch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                                 ctypes.c_int]),
     "imex_batch_get_row_launch": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]),
     "imex_batch_set_graph": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "imex_batch_kernel_launches": (ctypes.c_int64, [ctypes.c_void_p]),

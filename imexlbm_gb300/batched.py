@@ -50,7 +50,7 @@ def tau_of(edge, re, u0):
     return System(text=f"1.0 0.1 {re}\n{u0} 1 1\n{edge} {edge} {edge}\n").tau
 
 
-def run(n=64, steps=500, precision="f32", seed=20261203, log=print, check_fp64=True):
+def run(n=64, steps=500, precision="f32", seed=20261203, log=print, check_fp64=True, row_launch=None):
     import torch
 
     work = workload(n, seed, precision)
@@ -63,6 +63,8 @@ def run(n=64, steps=500, precision="f32", seed=20261203, log=print, check_fp64=T
         lats.append(lat)
     cells = sum(w["edge"] ** 3 for w in work)
     batch = Batch(max(2, n))
+    if row_launch is not None:
+        batch.set_row_launch(*row_launch)
     for lat in lats:
         batch.add(lat)
     m0 = [lat.Conserved()[0] for lat in lats]
@@ -80,7 +82,8 @@ def run(n=64, steps=500, precision="f32", seed=20261203, log=print, check_fp64=T
     mlups = cells * (steps - 1) / t_batch / 1e6
     result = {"lattices": n, "steps": steps, "precision": precision, "seed": seed, "cells": cells,
               "batch_mlups": mlups, "batch_seconds": t_batch, "warmup_seconds": t_warm,
-              "batch_launches_timed": launches, "launch_shape": batch.get_launch()}
+              "batch_launches_timed": launches, "launch_shape": batch.get_launch(),
+              "row_launch": batch.get_row_launch()}
     cons = [lat.Conserved() for lat in lats]
     if check_fp64:
         ke_err, drift, mom = [], [], []
@@ -116,9 +119,12 @@ def main(argv=None) -> int:
     ap.add_argument("--precision", choices=["f32", "f16dev", "mixed"], default="f32")
     ap.add_argument("--seed", type=int, default=20261203)
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--row-launch", default=None, metavar="STAGES,KB,CTAS",
+                    help="pin the row kernel's shape (-1,0,0: off) instead of autotuning it")
     ap.add_argument("--json", default=None)
     a = ap.parse_args(argv)
-    r = run(a.lattices, a.steps, a.precision, a.seed, check_fp64=not a.no_fp64)
+    rl = tuple(int(v) for v in a.row_launch.split(",")) if a.row_launch else None
+    r = run(a.lattices, a.steps, a.precision, a.seed, check_fp64=not a.no_fp64, row_launch=rl)
     if a.json:
         with open(a.json, "w") as fp:
             json.dump(r, fp, indent=1)

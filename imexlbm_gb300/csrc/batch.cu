@@ -39,10 +39,9 @@
 
 #include "imexlbm.h"
 #include "imexlbm_internal.hpp"
-#include "bulk.cuh"
-#include "eng_lowp.cuh"
 #include "lattice_internal.hpp"
 #include "lowp_math.cuh"
+#include "rows_lowp.cuh"
 
 namespace imex {
 
@@ -74,13 +73,9 @@ struct BatchHeader {
 
 // Table header of the row kernel's members.
 struct RowsHeader {
-    unsigned total;        // work items of all its members
-    int count;             // its members
-    unsigned stage_bytes;  // ring stage size (the largest member item)
-    int pad;
+    unsigned total;  // work items of all its members
+    int count;       // its members
 };
-
-constexpr int kBatchRowThreads = 256;
 
 template <int P>
 __device__ __forceinline__ void batch_cell(const BatchEntry& e, unsigned long long local, int s, const CollideF32& base)
@@ -109,12 +104,12 @@ __device__ __forceinline__ void batch_cell(const BatchEntry& e, unsigned long lo
     lowp::collide_dev_f32<P>(h, cp);
     if constexpr (P == IMEX_F16DEV) {
         auto at = [&](int a) -> T& { return dst[(size_t)a * e.plane + local]; };
-        if (e.sr) lowp::store_f16_cell_sr(h, lowp::sr_hash(local, e.seed + (uint32_t)s), at);
+        if (e.sr) lowp::store_f16_cell_sr(h, local, e.seed + (uint32_t)s, at);
         else lowp::store_f16_cell(h, at);
-        return;
-    }
+    } else {
 #pragma unroll
-    for (int a = 0; a < kQ; ++a) dst[(size_t)a * e.plane + local] = S::store(h[a], a);
+        for (int a = 0; a < kQ; ++a) dst[(size_t)a * e.plane + local] = S::store(h[a], a);
+    }
 }
 
 // CPT cells per thread, strided by blockDim within a chunk of CPT*blockDim.
@@ -148,136 +143,53 @@ __global__ void __launch_bounds__(256) k_batch(const BatchHeader* __restrict__ h
     }
 }
 
-// Row-staged batched step (see the file header and rows.cuh).  One CTA per
-// slot of the persistent grid walks items blockIdx.x, + gridDim.x, ...
-__global__ void __launch_bounds__(kBatchRowThreads, 1)
+// Row-staged batched step (rows_lowp.cuh): work items of every member in
+// one persistent loop; an item's member is found by binary search over the
+// members' first-item indices, kept in shared memory after the ring.
+template <int kDirBytes>
+__global__ void __launch_bounds__(rowslp::kThreads, 2)
     k_batch_rows(const RowsHeader* __restrict__ hdr, const BatchEntry* __restrict__ tab, int s, CollideF32 base,
                  int stages, unsigned* __restrict__ err)
 {
-    extern __shared__ __align__(128) unsigned char smem_raw[];
-    __shared__ unsigned sbegin[kBatchMax + 1];
-    uint64_t* full = reinterpret_cast<uint64_t*>(smem_raw);
-    unsigned char* ring = smem_raw + kRowBarrierBytes;
+    extern __shared__ __align__(128) unsigned char smem[];
     const int count = hdr->count;
     const unsigned total = hdr->total;
-    const unsigned stage_bytes = hdr->stage_bytes;
+    unsigned* sbegin = reinterpret_cast<unsigned*>(smem + rowslp::smem_bytes(kDirBytes, stages));
     for (int q = threadIdx.x; q < count; q += blockDim.x) sbegin[q] = tab[q].ibegin;
     if (threadIdx.x == 0) sbegin[count] = total;
     __syncthreads();
     const unsigned G = gridDim.x;
     const int my = blockIdx.x < total ? (int)((total - 1 - blockIdx.x) / G) + 1 : 0;
-    const int nwarps = blockDim.x >> 5;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int my_dir = warp + nwarps * lane;
-    const bool issuer = lane * nwarps < kQ && my_dir < kQ;
-
-    struct Item {
-        int m, x, y0;
-        bool active;
-    };
     auto item_of = [&](int t) {
-        const unsigned it = blockIdx.x + (unsigned)t * G;
-        int lo = 0, hi = count;  // largest lo with sbegin[lo] <= it
+        const unsigned itx = blockIdx.x + (unsigned)t * G;
+        int lo = 0, hi = count;  // largest lo with sbegin[lo] <= itx
         while (hi - lo > 1) {
             const int mid = (lo + hi) >> 1;
-            if (sbegin[mid] <= it) lo = mid;
+            if (sbegin[mid] <= itx) lo = mid;
             else hi = mid;
         }
         const BatchEntry& e = tab[lo];
-        const unsigned local = it - sbegin[lo];
+        rowslp::Item it;
+        const int cur = e.cur ^ (s & 1);
+        it.src = static_cast<const unsigned char*>(e.buf[cur]);
+        it.dst = static_cast<unsigned char*>(e.buf[cur ^ 1]);
+        it.plane = e.plane;
+        it.nx = e.nx;
+        it.ny = e.ny;
+        it.nz = e.nz;
+        it.B = e.B;
+        const unsigned local = itx - sbegin[lo];
         const unsigned yblocks = (unsigned)(e.ny / e.B);
-        Item r;
-        r.m = lo;
-        r.x = (int)(local / yblocks);
-        r.y0 = (int)(local - (unsigned)r.x * yblocks) * e.B;
-        r.active = s < e.steps;
-        return r;
+        it.x = (int)(local / yblocks);
+        it.y0 = (int)(local - (unsigned)it.x * yblocks) * e.B;
+        it.prec = e.prec;
+        it.eps = e.eps;
+        it.sr = e.sr;
+        it.seed = e.seed + (uint32_t)s;
+        it.active = s < e.steps;
+        return it;
     };
-    auto esize = [](int prec) { return prec == IMEX_F32 ? 4u : 2u; };
-    auto arm = [&](int t) {
-        const Item r = item_of(t);
-        const BatchEntry& e = tab[r.m];
-        const uint32_t bytes = r.active ? (uint32_t)kQ * e.B * e.nz * esize(e.prec) : 0u;
-        bulk::mbar_arrive_expect_tx(&full[t % stages], bytes);
-    };
-    auto issue = [&](int t) {
-        if (!issuer) return;
-        const Item r = item_of(t);
-        if (!r.active) return;
-        const BatchEntry& e = tab[r.m];
-        const uint32_t es = esize(e.prec);
-        const int B = e.B, nz = e.nz, ny = e.ny;
-        const uint32_t row_bytes = (uint32_t)nz * es;
-        const int a = my_dir;
-        int xs = r.x - ex(a, 0);
-        xs = xs < 0 ? xs + e.nx : xs >= e.nx ? xs - e.nx : xs;
-        const unsigned char* src = static_cast<const unsigned char*>(e.buf[e.cur ^ (s & 1)]);
-        const unsigned char* plane = src + ((size_t)a * e.plane + (size_t)xs * ny * nz) * es;
-        unsigned char* st = ring + (size_t)(t % stages) * stage_bytes + (size_t)a * B * row_bytes;
-        uint64_t* bar = &full[t % stages];
-        const int lo = r.y0 - ex(a, 1);
-        if (lo < 0) {
-            bulk::copy_g2s(st, plane + (size_t)(ny - 1) * row_bytes, row_bytes, bar);
-            if (B > 1) bulk::copy_g2s(st + row_bytes, plane, (uint32_t)(B - 1) * row_bytes, bar);
-        } else if (lo + B > ny) {
-            if (B > 1) bulk::copy_g2s(st, plane + (size_t)lo * row_bytes, (uint32_t)(B - 1) * row_bytes, bar);
-            bulk::copy_g2s(st + (size_t)(B - 1) * row_bytes, plane, row_bytes, bar);
-        } else {
-            bulk::copy_g2s(st, plane + (size_t)lo * row_bytes, (uint32_t)B * row_bytes, bar);
-        }
-    };
-
-    if (threadIdx.x == 0) {
-        for (int q = 0; q < stages; ++q) bulk::mbar_init(&full[q], 1);
-        bulk::fence_mbar_init();
-        for (int t = 0; t < stages && t < my; ++t) arm(t);
-    }
-    __syncthreads();
-    for (int t = 0; t < stages - 1 && t < my; ++t) issue(t);
-
-    for (int t = 0; t < my; ++t) {
-        if (t + stages - 1 < my) issue(t + stages - 1);
-        const int st_i = t % stages;
-        const int ok = bulk::mbar_wait(&full[st_i], (uint32_t)((t / stages) & 1));
-        if (__syncthreads_or(!ok)) {
-            if (threadIdx.x == 0) {
-                atomicOr(err, 1u);
-                const int last = t + stages - 1 < my ? t + stages - 1 : my - 1;
-                for (int q = t; q <= last; ++q) bulk::mbar_wait(&full[q % stages], (uint32_t)((q / stages) & 1));
-            }
-            __syncthreads();
-            return;
-        }
-        const Item r = item_of(t);
-        if (r.active) {
-            const BatchEntry& e = tab[r.m];
-            CollideF32 cp = base;
-            cp.eps = e.eps;
-            cp.sr = e.sr;
-            cp.seed = e.seed + (uint32_t)s;
-            const unsigned char* stg = ring + (size_t)st_i * stage_bytes;
-            void* dst = e.buf[e.cur ^ (s & 1) ^ 1];
-            const int nz = e.nz, n = e.B * nz, astride = e.B * nz;
-            const size_t row0 = ((size_t)r.x * e.ny + r.y0) * nz;  // first cell of the item
-            if (e.prec == IMEX_F32) {
-                const EngLowp<IMEX_F32> eng{cp};
-                for (int q = threadIdx.x; q < n; q += blockDim.x) {
-                    const int b = q / nz, z = q - b * nz;
-                    eng.run(reinterpret_cast<const float*>(stg) + (size_t)b * nz, astride, nz, z,
-                            static_cast<float*>(dst), e.plane, row0 + (size_t)b * nz);
-                }
-            } else {
-                const EngLowp<IMEX_F16DEV> eng{cp};
-                for (int q = threadIdx.x; q < n; q += blockDim.x) {
-                    const int b = q / nz, z = q - b * nz;
-                    eng.run(reinterpret_cast<const __half*>(stg) + (size_t)b * nz, astride, nz, z,
-                            static_cast<__half*>(dst), e.plane, row0 + (size_t)b * nz);
-                }
-            }
-        }
-        if (threadIdx.x == 0 && t + stages < my) arm(t + stages);
-        __syncthreads();
-    }
+    rowslp::run_items<kDirBytes, lowp::F2>(item_of, my, stages, base, smem, err);
 }
 
 }  // namespace
@@ -286,11 +198,12 @@ __global__ void __launch_bounds__(kBatchRowThreads, 1)
 
 using namespace imex;
 
-// Row-kernel launch shape: ring depth, stage size and resident CTAs per SM
-// (stages 0: not chosen yet; -1: row kernel off, every member in the cell
-// kernel).
+// Row-kernel launch shape: ring depth, KiB per direction in a stage (1, 2
+// or 4), resident CTAs per SM (stages 0: not chosen yet; -1: row kernel
+// off, every member in the cell kernel) and whether float32 members join
+// it (float16-deviation members always do when their rows allow).
 struct RowShape {
-    int stages = 0, stage_kb = 0, ctas_per_sm = 0;
+    int stages = 0, dir_kb = 0, ctas_per_sm = 0, f32 = 1;
 };
 
 struct BatchShape {
@@ -353,9 +266,19 @@ CollideF32 base_constants()
     return make_collide_f32(0.0);
 }
 
-// Dynamic shared memory the row kernel may use (227 KB per CTA less its
-// static member table).
-constexpr int kRowsDynMax = 227 * 1024 - (int)sizeof(unsigned) * (kBatchMax + 1) - 1024;
+// Shared memory of a row-kernel CTA: barriers, ring and the table of the
+// members' first items.
+size_t rows_smem(const RowShape& rs, int members)
+{
+    return rowslp::smem_bytes(rs.dir_kb * 1024, rs.stages) + ((sizeof(unsigned) * (members + 1) + 15) & ~15ull);
+}
+
+// Whether the row shape's CTAs fit an SM's shared memory.
+bool rows_fit(const RowShape& rs, int members)
+{
+    const size_t smem = rows_smem(rs, members);
+    return smem <= 227 * 1024 && (size_t)rs.ctas_per_sm * (smem + 1024) <= 228 * 1024;
+}
 
 int kinds(const imex_batch* b) { return (b->n_cell > 0 ? 1 : 0) | (b->n_row > 0 ? 2 : 0); }
 
@@ -379,8 +302,23 @@ cudaError_t launch_step(imex_batch* b, const BatchShape& sh, const RowShape& rs,
         const unsigned items = b->h_rhdr->total;
         unsigned grid = (unsigned)(b->sms * rs.ctas_per_sm);
         if (grid > items) grid = items;
-        const size_t smem = kRowBarrierBytes + (size_t)rs.stages * b->h_rhdr->stage_bytes;
-        k_batch_rows<<<grid, kBatchRowThreads, smem, b->stream>>>(b->d_rhdr, b->d_rtab, s, base, rs.stages, b->d_err);
+        if (!rows_fit(rs, b->n_row)) return cudaErrorInvalidValue;
+        const size_t smem = rows_smem(rs, b->n_row);
+        switch (rs.dir_kb) {
+        case 1:
+            k_batch_rows<1024><<<grid, rowslp::kThreads, smem, b->stream>>>(b->d_rhdr, b->d_rtab, s, base, rs.stages,
+                                                                            b->d_err);
+            break;
+        case 2:
+            k_batch_rows<2048><<<grid, rowslp::kThreads, smem, b->stream>>>(b->d_rhdr, b->d_rtab, s, base, rs.stages,
+                                                                            b->d_err);
+            break;
+        case 4:
+            k_batch_rows<4096><<<grid, rowslp::kThreads, smem, b->stream>>>(b->d_rhdr, b->d_rtab, s, base, rs.stages,
+                                                                            b->d_err);
+            break;
+        default: return cudaErrorInvalidValue;
+        }
         return cudaGetLastError();
     }
     return cudaSuccess;
@@ -399,12 +337,12 @@ int64_t owed(const imex_batch* b, size_t m, int64_t want)
 // the member stays in the cell kernel.
 int rows_per_item(const imex_lattice* h, const RowShape& rs)
 {
-    if (rs.stages <= 0) return 0;
+    if (rs.stages <= 0 || (h->precision == IMEX_F32 && !rs.f32)) return 0;
     const size_t row_bytes = (size_t)h->g.nz * lattice_elem_size(h->precision);
-    const size_t cap = (size_t)rs.stage_kb * 1024;
-    if (row_bytes % 16 || (size_t)kQ * row_bytes > cap) return 0;
+    const size_t cap = (size_t)rs.dir_kb * 1024;
+    if (row_bytes % 16 || row_bytes > cap) return 0;
     if ((size_t)h->g.nx * h->g.ny >= 0x7fffffffu) return 0;
-    for (int B = (int)std::min<size_t>((size_t)h->g.ny, cap / ((size_t)kQ * row_bytes)); B > 1; --B)
+    for (int B = (int)std::min<size_t>((size_t)h->g.ny, cap / row_bytes); B > 1; --B)
         if (h->g.ny % B == 0) return B;
     return 1;
 }
@@ -414,7 +352,7 @@ int rows_per_item(const imex_lattice* h, const RowShape& rs)
 int upload_table(imex_batch* b, const std::vector<int>& steps, const RowShape& rs)
 {
     unsigned long long begin = 0;
-    unsigned ibegin = 0, stage_bytes = 0;
+    unsigned ibegin = 0;
     int n = 0, nr = 0;
     for (size_t m = 0; m < b->members.size(); ++m) {
         imex_lattice* h = b->members[m];
@@ -438,7 +376,6 @@ int upload_table(imex_batch* b, const std::vector<int>& steps, const RowShape& r
             e.begin = 0;
             e.ibegin = ibegin;
             ibegin += (unsigned)((size_t)h->g.nx * (h->g.ny / B));
-            stage_bytes = std::max(stage_bytes, (unsigned)(kQ * B * h->g.nz * lattice_elem_size(h->precision)));
         } else {
             e.begin = begin;
             e.ibegin = 0;
@@ -449,7 +386,6 @@ int upload_table(imex_batch* b, const std::vector<int>& steps, const RowShape& r
     b->h_hdr->count = n;
     b->h_rhdr->total = ibegin;
     b->h_rhdr->count = nr;
-    b->h_rhdr->stage_bytes = stage_bytes;
     b->n_cell = n;
     b->n_row = nr;
     B_CUDA(b, cudaMemcpyAsync(b->d_tab, b->h_tab, sizeof(BatchEntry) * (n ? n : 1), cudaMemcpyHostToDevice, b->stream),
@@ -503,18 +439,17 @@ std::vector<BatchShape> candidates()
     return out;
 }
 
-// Row-kernel shapes: (stages, stage KB) per resident-CTA count, within the
-// shared memory of an SM.
+// Row-kernel shapes (stages, KiB per direction, CTAs per SM); those whose
+// CTAs do not fit an SM's shared memory with the batch's table are skipped.
 std::vector<RowShape> row_candidates()
 {
-    const int shapes[][3] = {{1, 2, 32}, {1, 3, 32}, {1, 4, 32}, {1, 2, 64}, {1, 3, 64}, {1, 2, 100},
-                             {2, 2, 24}, {2, 3, 24}, {2, 4, 24}, {2, 2, 48}, {3, 2, 16}, {3, 3, 16}};
+    const int shapes[][3] = {{2, 2, 2}, {2, 1, 2}, {3, 1, 2}, {2, 2, 1}, {3, 2, 1}, {2, 4, 1}};
     std::vector<RowShape> out;
     for (const auto& x : shapes) {
         RowShape r;
-        r.ctas_per_sm = x[0];
-        r.stages = x[1];
-        r.stage_kb = x[2];
+        r.stages = x[0];
+        r.dir_kb = x[1];
+        r.ctas_per_sm = x[2];
         out.push_back(r);
     }
     return out;
@@ -553,7 +488,7 @@ int time_step(imex_batch* b, const BatchShape& sh, const RowShape& rs, float* ms
 // by imex_batch_set_launch / imex_batch_set_row_launch are kept.
 int tune_batch(imex_batch* b, bool tune_cells, bool tune_rows)
 {
-    const RowShape off{-1, 0, 0};
+    const RowShape off{-1, 0, 0, 1};
     float best = 0.f;
     if (tune_cells) {
         BatchShape best_shape;
@@ -572,13 +507,17 @@ int tune_batch(imex_batch* b, bool tune_cells, bool tune_rows)
         int rc = time_step(b, b->shape, off, &best);
         if (rc) return rc;
         RowShape best_rs = off;
-        for (const RowShape& rs : row_candidates()) {
-            float ms = 0.f;
-            rc = time_step(b, b->shape, rs, &ms);
-            if (rc) return rc;
-            if (b->n_row > 0 && ms < best) {
-                best = ms;
-                best_rs = rs;
+        for (RowShape rs : row_candidates()) {
+            if (!rows_fit(rs, (int)b->members.size())) continue;
+            for (int f32 = 1; f32 >= 0; --f32) {
+                rs.f32 = f32;
+                float ms = 0.f;
+                rc = time_step(b, b->shape, rs, &ms);
+                if (rc) return rc;
+                if (b->n_row > 0 && ms < best) {
+                    best = ms;
+                    best_rs = rs;
+                }
             }
         }
         b->rshape = best_rs;
@@ -613,7 +552,8 @@ bool graph_valid(const imex_batch* b, int K)
 {
     return b->graph && b->graph_k == K && b->graph_shape.threads == b->shape.threads &&
            b->graph_shape.cpt == b->shape.cpt && b->graph_shape.ctas_per_sm == b->shape.ctas_per_sm &&
-           b->graph_rshape.stages == b->rshape.stages && b->graph_rshape.stage_kb == b->rshape.stage_kb &&
+           b->graph_rshape.stages == b->rshape.stages && b->graph_rshape.dir_kb == b->rshape.dir_kb &&
+           b->graph_rshape.f32 == b->rshape.f32 &&
            b->graph_rshape.ctas_per_sm == b->rshape.ctas_per_sm && b->graph_kinds == kinds(b);
 }
 
@@ -644,7 +584,11 @@ int imex_batch_create(int max_members, imex_batch** out)
     if (e == cudaSuccess) e = cudaMalloc(&b->d_err, sizeof(unsigned));
     if (e == cudaSuccess) e = cudaMemset(b->d_err, 0, sizeof(unsigned));
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_batch_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, kRowsDynMax);
+        e = cudaFuncSetAttribute(k_batch_rows<1024>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_batch_rows<2048>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_batch_rows<4096>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
     if (e != cudaSuccess) {
         imex_batch_destroy(b);
         cudaGetLastError();
@@ -802,29 +746,29 @@ int imex_batch_get_launch(imex_batch* b, int out[3])
     return IMEX_OK;
 }
 
-int imex_batch_set_row_launch(imex_batch* b, int stages, int stage_kb, int ctas_per_sm)
+int imex_batch_set_row_launch(imex_batch* b, int stages, int dir_kb, int ctas_per_sm, int float32_members)
 {
     if (!b) return set_thread_error(IMEX_ERR_ARG, "imex_batch_set_row_launch: null batch");
     if (stages == 0 || stages == -1) {  // 0: autotune, -1: row kernel off
-        b->rshape = RowShape{stages, 0, 0};
+        b->rshape = RowShape{stages, 0, 0, 1};
         return IMEX_OK;
     }
-    if (stages < 2 || stages > 8 || stage_kb < 4 || ctas_per_sm < 1 || ctas_per_sm > 4 ||
-        (size_t)stages * stage_kb * 1024 + kRowBarrierBytes > (size_t)kRowsDynMax ||
-        ctas_per_sm * ((size_t)stages * stage_kb * 1024 + kRowBarrierBytes + sizeof(unsigned) * (kBatchMax + 1) + 1024) >
-            228 * 1024)
-        return bfail(b, IMEX_ERR_ARG, "imex_batch_set_row_launch: 2 <= stages <= 8, stage_kb >= 4, 1 <= ctas_per_sm "
-                                      "<= 4, and the CTAs' rings must fit an SM's shared memory");
-    b->rshape = RowShape{stages, stage_kb, ctas_per_sm};
+    const RowShape rs{stages, dir_kb, ctas_per_sm, float32_members ? 1 : 0};
+    if (stages < 2 || stages > 8 || (dir_kb != 1 && dir_kb != 2 && dir_kb != 4) || ctas_per_sm < 1 ||
+        ctas_per_sm > 4 || !rows_fit(rs, b->capacity))
+        return bfail(b, IMEX_ERR_ARG, "imex_batch_set_row_launch: 2 <= stages <= 8, dir_kb 1, 2 or 4, 1 <= "
+                                      "ctas_per_sm <= 4, and the CTAs' rings must fit an SM's shared memory");
+    b->rshape = rs;
     return IMEX_OK;
 }
 
-int imex_batch_get_row_launch(imex_batch* b, int out[3])
+int imex_batch_get_row_launch(imex_batch* b, int out[4])
 {
     if (!b || !out) return set_thread_error(IMEX_ERR_ARG, "imex_batch_get_row_launch: null argument");
     out[0] = b->rshape.stages;
-    out[1] = b->rshape.stage_kb;
+    out[1] = b->rshape.dir_kb;
     out[2] = b->rshape.ctas_per_sm;
+    out[3] = b->rshape.f32;
     return IMEX_OK;
 }
 

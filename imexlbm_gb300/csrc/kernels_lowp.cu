@@ -8,8 +8,8 @@
 
 #include "kernels_lowp.cuh"
 #include "lowp_math.cuh"
-#include "eng_lowp.cuh"
 #include "rows.cuh"
+#include "rows_lowp.cuh"
 #include "tg_init.cuh"
 
 namespace imex {
@@ -46,7 +46,7 @@ __global__ void __launch_bounds__(kStepBlock) k_step_lowp(const typename Storage
     collide_dev_f32<P>(h, cp);
     if constexpr (P == IMEX_F16DEV) {
         auto at = [&](int a) -> __half& { return dst[(size_t)a * g.plane + cell]; };
-        if (cp.sr) lowp::store_f16_cell_sr(h, lowp::sr_hash(cell, cp.seed), at);
+        if (cp.sr) lowp::store_f16_cell_sr(h, cell, cp.seed, at);
         else lowp::store_f16_cell(h, at);
         return;
     }
@@ -220,16 +220,42 @@ cudaError_t launch_step_lowp(int prec, int mode, const void* src, void* dst, con
 
 bool rows_lowp_eligible(int prec, const Geom& g)
 {
-    return prec == IMEX_F32 ? rows_eligible<float>(g) : rows_eligible<__half>(g);
+    const size_t row = (size_t)g.nz * (prec == IMEX_F32 ? 4 : 2);
+    return row % 16 == 0 && row <= (size_t)kRowsLowpDirMax && (size_t)g.nx * g.ny < 0x7fffffffu;
+}
+
+template <int D>
+cudaError_t launch_rows_lowp_d(int prec, const void* src, void* dst, const Geom& g, const CollideF32& cp,
+                               const RowConfig& rc, unsigned* err, cudaStream_t s, unsigned grid)
+{
+    const size_t smem = rowslp::smem_bytes(D, rc.stages);
+    cudaError_t e = cudaFuncSetAttribute(rowslp::k_rows_lowp<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    rowslp::k_rows_lowp<D><<<grid, rowslp::kThreads, smem, s>>>(src, dst, g, prec, rc.rows, cp, rc.stages, err);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_rows_lowp(int prec, const void* src, void* dst, const Geom& g, const CollideF32& cp,
                              const RowConfig& rc, unsigned* err, cudaStream_t s)
 {
-    if (prec == IMEX_F32)
-        return launch_rows(static_cast<const float*>(src), static_cast<float*>(dst), g, EngLowp<IMEX_F32>{cp}, rc, err, s);
-    return launch_rows(static_cast<const __half*>(src), static_cast<__half*>(dst), g, EngLowp<IMEX_F16DEV>{cp}, rc,
-                       err, s);
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    }
+    const size_t es = prec == IMEX_F32 ? 4 : 2;
+    if (rc.rows < 1 || g.ny % rc.rows || (size_t)rc.rows * g.nz * es > (size_t)rc.dir_bytes || rc.stages < 2)
+        return cudaErrorInvalidValue;
+    const long long items = (long long)g.nx * (g.ny / rc.rows);
+    long long grid = (long long)sms * rc.ctas_per_sm;
+    if (grid > items) grid = items;
+    switch (rc.dir_bytes) {
+    case 1024: return launch_rows_lowp_d<1024>(prec, src, dst, g, cp, rc, err, s, (unsigned)grid);
+    case 2048: return launch_rows_lowp_d<2048>(prec, src, dst, g, cp, rc, err, s, (unsigned)grid);
+    case 4096: return launch_rows_lowp_d<4096>(prec, src, dst, g, cp, rc, err, s, (unsigned)grid);
+    default: return cudaErrorInvalidValue;
+    }
 }
 
 size_t rows_lowp_stage_bytes(int prec, int nz) { return (size_t)kQ * nz * (prec == IMEX_F32 ? 4 : 2); }

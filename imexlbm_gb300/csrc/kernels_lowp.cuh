@@ -23,6 +23,8 @@ struct CollideF32 {
 CollideF32 make_collide_f32(double tau0);
 
 struct RowConfig;
+// Largest bytes per direction in a stage of the reduced-precision row kernel.
+constexpr int kRowsLowpDirMax = 4096;
 bool rows_lowp_eligible(int prec, const Geom& g);
 size_t rows_lowp_stage_bytes(int prec, int nz);
 cudaError_t launch_rows_lowp(int prec, const void* src, void* dst, const Geom& g, const CollideF32& cp,

@@ -32,6 +32,7 @@
 #include "kernels_lowp.cuh"
 #include "rows.cuh"
 #include "lattice_internal.hpp"
+#include "rows_lowp.cuh"
 
 namespace imex {
 
@@ -84,7 +85,7 @@ bool use_fixed(const imex_lattice* h)
 
 double* dbuf(imex_lattice* h, int which) { return static_cast<double*>(h->buf[which]); }
 
-bool lowp(const imex_lattice* h) { return h->precision != IMEX_F64; }
+bool is_lowp(const imex_lattice* h) { return h->precision != IMEX_F64; }
 
 // ------------------------------------------------------------ launch shapes --
 // The fused step has two kernels: one thread per cell with direct pulls
@@ -96,16 +97,47 @@ bool lowp(const imex_lattice* h) { return h->precision != IMEX_F64; }
 
 bool rows_eligible_for(const imex_lattice* h)
 {
-    if (lowp(h)) return rows_lowp_eligible(h->precision, h->g);
+    if (is_lowp(h)) return rows_lowp_eligible(h->precision, h->g);
     return use_fixed(h) && rows_fx_eligible(h->g);
 }
 
 size_t stage_bytes(const imex_lattice* h) { return (size_t)kQ * h->g.nz * elem_size(h->precision); }
 
+// Reduced precision: the smallest direction block (1, 2 or 4 KB) of a stage
+// that holds B rows; 0 if none does.
+int lowp_dir_bytes(const imex_lattice* h, int B)
+{
+    const size_t need = (size_t)B * h->g.nz * elem_size(h->precision);
+    return need <= 1024 ? 1024 : need <= 2048 ? 2048 : need <= 4096 ? 4096 : 0;
+}
+
 std::vector<RowConfig> row_candidates(const imex_lattice* h)
 {
     std::vector<RowConfig> out;
     if (!rows_eligible_for(h)) return out;
+    if (is_lowp(h)) {
+        // (stages, CTAs per SM) per direction block; B the most rows it holds
+        const int shapes[][2] = {{2, 2}, {3, 2}, {2, 1}, {3, 1}, {4, 1}};
+        const size_t row = (size_t)h->g.nz * elem_size(h->precision);
+        for (int dir : {1024, 2048, 4096}) {
+            if (row > (size_t)dir) continue;
+            int B = (int)std::min<size_t>((size_t)h->g.ny, dir / row);
+            while (h->g.ny % B) --B;
+            if (lowp_dir_bytes(h, B) != dir) continue;  // same items as a smaller block
+            for (const auto& sh : shapes) {
+                const size_t smem = rowslp::smem_bytes(dir, sh[0]);
+                if (smem > 227 * 1024 || (size_t)sh[1] * (smem + 1024) > 228 * 1024) continue;
+                RowConfig rc;
+                rc.stages = sh[0];
+                rc.ctas_per_sm = sh[1];
+                rc.rows = B;
+                rc.dir_bytes = dir;
+                rc.threads = rowslp::kThreads;
+                out.push_back(rc);
+            }
+        }
+        return out;
+    }
     const size_t sb = stage_bytes(h);  // one row of all 27 directions
     const size_t per_sm = 227 * 1024;
     const int threads = h->g.nz >= 256 ? 256 : ((h->g.nz + 31) / 32) * 32;
@@ -113,7 +145,7 @@ std::vector<RowConfig> row_candidates(const imex_lattice* h)
     const int stage_opts[3] = {2, 3, 4};
     const int rows_opts[4] = {1, 2, 4, 8};
     for (int c : ctas_opts) {
-        if (!lowp(h) && c > 2) continue;  // fixed-point engine: 128+ registers per thread
+        if (!is_lowp(h) && c > 2) continue;  // fixed-point engine: 128+ registers per thread
         for (int B : rows_opts) {
             if (h->g.ny % B) continue;
             for (int s : stage_opts) {
@@ -143,14 +175,14 @@ std::tuple<int, int, int, int, int> tune_key(const imex_lattice* h)
 
 cudaError_t launch_fused_rows(imex_lattice* h, const void* src, void* dst, const RowConfig& rc)
 {
-    if (lowp(h)) return launch_rows_lowp(h->precision, src, dst, h->g, h->cf32, rc, h->d_err, h->stream);
+    if (is_lowp(h)) return launch_rows_lowp(h->precision, src, dst, h->g, h->cf32, rc, h->d_err, h->stream);
     return launch_rows_fx(static_cast<const double*>(src), static_cast<double*>(dst), h->g, h->fx, h->cf64,
                           h->d_fallback, rc, h->d_err, h->stream);
 }
 
 cudaError_t launch_fused_classic(imex_lattice* h, const void* src, void* dst)
 {
-    if (lowp(h)) return launch_step_lowp(h->precision, kModeFused, src, dst, h->g, h->cf32, h->stream);
+    if (is_lowp(h)) return launch_step_lowp(h->precision, kModeFused, src, dst, h->g, h->cf32, h->stream);
     if (use_fixed(h))
         return launch_step_fx(kModeFused, static_cast<const double*>(src), static_cast<double*>(dst), h->g, h->fx,
                               h->cf64, h->d_fallback, h->stream);
@@ -258,7 +290,7 @@ int launch_mode(imex_lattice* h, int mode)
     PhaseScope timed(h->prof, mode == kModeStream ? IMEX_PHASE_STREAM : IMEX_PHASE_COLLISION, h->stream);
     if (mode == kModeFused && h->rows.stages > 0)
         e = launch_fused_rows(h, src, dst, h->rows);
-    else if (lowp(h))
+    else if (is_lowp(h))
         e = launch_step_lowp(h->precision, mode, src, dst, h->g, h->cf32, h->stream);
     else if (mode != kModeStream && use_fixed(h))
         e = launch_step_fx(mode, src, dst, h->g, h->fx, h->cf64, h->d_fallback, h->stream);
@@ -444,7 +476,7 @@ int imex_initialize_phase(imex_lattice* h, double phx, double phy, double phz)
     cudaError_t e = cudaMallocAsync(&dev, tot * sizeof(double), h->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(dev, host, tot * sizeof(double), cudaMemcpyHostToDevice, h->stream);
     if (e == cudaSuccess)
-        e = lowp(h) ? launch_init_lowp(h->precision, h->buf[0], h->g, dev + offs[0], dev + offs[1], dev + offs[2], h->rho0,
+        e = is_lowp(h) ? launch_init_lowp(h->precision, h->buf[0], h->g, dev + offs[0], dev + offs[1], dev + offs[2], h->rho0,
                                        h->u0, h->stream)
                     : launch_init_f64(dbuf(h, 0), h->g, dev + offs[0], dev + offs[1], dev + offs[2], h->rho0, h->u0,
                                       h->stream);
@@ -504,7 +536,7 @@ int imex_conserved(imex_lattice* h, double out[5])
     const bool pull = h->tag == kPendingStream;
     int timed = h->prof.start(IMEX_PHASE_CONSERVED, h->stream);
     cudaError_t e =
-        lowp(h) ? launch_conserved_lowp(h->precision, pull, h->buf[h->cur], h->g, h->d_partial, h->d_out, h->stream)
+        is_lowp(h) ? launch_conserved_lowp(h->precision, pull, h->buf[h->cur], h->g, h->d_partial, h->d_out, h->stream)
         : use_fixed(h) ? launch_conserved_fx(pull, dbuf(h, h->cur), h->g, h->fx, h->d_partial, h->d_out, h->stream)
                        : launch_conserved_f64(pull, dbuf(h, h->cur), h->g, h->d_partial, h->d_out, h->stream);
     h->prof.stop(timed, h->stream);
@@ -534,7 +566,7 @@ int macro_fields(imex_lattice* h, double* p, double* u, double* v, double* w)
 {
     const bool pull = h->tag == kPendingStream;
     PhaseScope timed(h->prof, IMEX_PHASE_MACRO, h->stream);
-    cudaError_t e = lowp(h) ? launch_macro_lowp(h->precision, pull, h->buf[h->cur], h->g, p, u, v, w, h->stream)
+    cudaError_t e = is_lowp(h) ? launch_macro_lowp(h->precision, pull, h->buf[h->cur], h->g, p, u, v, w, h->stream)
                             : launch_macro_f64(pull, dbuf(h, h->cur), h->g, p, u, v, w, h->stream);
     if (e != cudaSuccess) return cuda_fail(h, e, "macroscopic kernel launch");
     ++h->launches;
@@ -606,7 +638,7 @@ static int get_f_impl(imex_lattice* h, double* dst, size_t n, cudaMemcpyKind kin
     int rc = check_ready(h, what);
     if (rc) return rc;
     if (!dst || n != (size_t)kQ * h->ncells) return fail(h, IMEX_ERR_ARG, std::string(what) + ": buffer size must be 27*nx*ny*nz");
-    if (lowp(h)) {
+    if (is_lowp(h)) {
         // convert (pulling through a pending streaming) into a float64 buffer
         double* tmp = dst;
         if (kind != cudaMemcpyDeviceToDevice)
@@ -631,7 +663,7 @@ static int set_f_impl(imex_lattice* h, const double* src, size_t n, cudaMemcpyKi
     if (!h) return set_thread_error(IMEX_ERR_ARG, std::string(what) + ": null handle");
     if (!src || n != (size_t)kQ * h->ncells) return fail(h, IMEX_ERR_ARG, std::string(what) + ": buffer size must be 27*nx*ny*nz");
     IMEX_CUDA(h, cudaSetDevice(h->device), "cudaSetDevice");
-    if (lowp(h)) {
+    if (is_lowp(h)) {
         const double* dsrc = src;
         double* tmp = nullptr;
         cudaError_t e = cudaSuccess;
@@ -669,7 +701,7 @@ int imex_set_engine(imex_lattice* h, int engine)
     if (!h) return set_thread_error(IMEX_ERR_ARG, "imex_set_engine: null handle");
     if (engine != IMEX_ENGINE_AUTO && engine != IMEX_ENGINE_NATIVE && engine != IMEX_ENGINE_FIXED)
         return fail(h, IMEX_ERR_ARG, "imex_set_engine: unknown engine");
-    if (engine == IMEX_ENGINE_FIXED && (!h->fx_ok || lowp(h)))
+    if (engine == IMEX_ENGINE_FIXED && (!h->fx_ok || is_lowp(h)))
         return fail(h, IMEX_ERR_ARG, "imex_set_engine: the fixed-point engine needs float64 storage and 0.75 <= rho0 <= 1.25");
     h->engine = engine;
     return IMEX_OK;
@@ -738,13 +770,21 @@ int imex_set_launch(imex_lattice* h, int stages, int rows_per_stage, int ctas_pe
                                      "bytes and a fixed-point or reduced-precision engine");
     const int B = rows_per_stage < 1 ? 1 : rows_per_stage;
     if (h->g.ny % B) return fail(h, IMEX_ERR_ARG, "imex_set_launch: rows_per_stage must divide ny");
-    if (stages < 2 || stages > 16 || kRowBarrierBytes + (size_t)stages * B * stage_bytes(h) > 227 * 1024)
-        return fail(h, IMEX_ERR_ARG, "imex_set_launch: ring does not fit in shared memory (2 <= stages <= 16)");
     RowConfig rc;
     rc.stages = stages;
     rc.rows = B;
     rc.ctas_per_sm = ctas_per_sm < 1 ? 1 : ctas_per_sm;
-    rc.threads = h->g.nz >= 256 ? 256 : ((h->g.nz + 31) / 32) * 32;
+    if (is_lowp(h)) {
+        rc.dir_bytes = lowp_dir_bytes(h, B);
+        rc.threads = rowslp::kThreads;
+        if (!rc.dir_bytes || stages < 2 || stages > 16 || rowslp::smem_bytes(rc.dir_bytes, stages) > 227 * 1024)
+            return fail(h, IMEX_ERR_ARG, "imex_set_launch: ring does not fit in shared memory (2 <= stages <= 16, "
+                                         "rows_per_stage * nz * element size <= 4096 bytes)");
+    } else {
+        if (stages < 2 || stages > 16 || kRowBarrierBytes + (size_t)stages * B * stage_bytes(h) > 227 * 1024)
+            return fail(h, IMEX_ERR_ARG, "imex_set_launch: ring does not fit in shared memory (2 <= stages <= 16)");
+        rc.threads = h->g.nz >= 256 ? 256 : ((h->g.nz + 31) / 32) * 32;
+    }
     h->rows = rc;
     h->shape_mode = 1;
     h->shape_pinned = true;

@@ -53,12 +53,15 @@ __device__ __forceinline__ uint32_t sr_hash(unsigned long long idx, uint32_t see
     return x;
 }
 
-// Random word k of a cell: the Weyl sequence r0 + k * phi (mod 2^32, phi =
-// 2^32 / golden ratio) from the cell's hash r0.  Each word is uniform
-// because r0 is; across a cell's words the draws are stratified rather
-// than independent, which if anything lowers the variance of the cell's
-// summed rounding error.
-__device__ __forceinline__ uint32_t sr_bits(uint32_t cell_hash, int k) { return cell_hash + (uint32_t)k * 0x9E3779B9u; }
+// Random bits of the stochastic rounding, shared by every kernel so that a
+// lattice's result does not depend on which kernel stepped it: cells 2p and
+// 2p + 1 of a lattice (flat index, z fastest) share the 32-bit word
+// sr_word(hash(p, step), a) = hash + a * phi for direction a (phi = 2^32 /
+// golden ratio, a Weyl sequence: each word uniform because the hash is;
+// across a pair's directions the draws are stratified rather than
+// independent).  Cell 2p takes bits 0..12 and cell 2p + 1 bits 16..28 -
+// the operand layout of cvt.rs.f16x2.f32 with cell 2p in the low half.
+__device__ __forceinline__ uint32_t sr_word(uint32_t pair_hash, int a) { return pair_hash + (uint32_t)a * 0x9E3779B9u; }
 
 // Store 27 float16 deviations of one cell, converting two at a time
 // (values already on the float16 grid convert exactly).
@@ -91,19 +94,20 @@ __device__ __forceinline__ uint32_t cvt_rs_f16x2(float hi, float lo, uint32_t rb
     return d;
 }
 
-// Store 27 float16 deviations of one cell with stochastic rounding: pair
-// (a, a + 1) draws the 32-bit word sr_bits(cell_hash, a / 2).
+// Store 27 float16 deviations of one cell with stochastic rounding: the
+// cell's half of its pair's random words (see sr_word).
 template <class Dst>
-__device__ __forceinline__ void store_f16_cell_sr(const float (&y)[kQ], uint32_t cell_hash, Dst&& at)
+__device__ __forceinline__ void store_f16_cell_sr(const float (&y)[kQ], unsigned long long cell, uint32_t seed,
+                                                  Dst&& at)
 {
+    const uint32_t ph = sr_hash(cell >> 1, seed);
+    const bool odd = cell & 1;
 #pragma unroll
-    for (int a = 0; a + 1 < kQ; a += 2) {
-        const uint32_t d = cvt_rs_f16x2(y[a + 1], y[a], sr_bits(cell_hash, a >> 1));
-        at(a) = __ushort_as_half((unsigned short)(d & 0xffffu));
-        at(a + 1) = __ushort_as_half((unsigned short)(d >> 16));
+    for (int a = 0; a < kQ; ++a) {
+        const uint32_t w = sr_word(ph, a);
+        const uint32_t d = odd ? cvt_rs_f16x2(y[a], 0.0f, w) >> 16 : cvt_rs_f16x2(0.0f, y[a], w) & 0xffffu;
+        at(a) = __ushort_as_half((unsigned short)d);
     }
-    const uint32_t d = cvt_rs_f16x2(0.0f, y[kQ - 1], sr_bits(cell_hash, kQ >> 1));
-    at(kQ - 1) = __ushort_as_half((unsigned short)(d & 0xffffu));
 }
 
 // kScale: the collision works on kScale * (f - w).  float32 storage keeps f
@@ -122,6 +126,7 @@ struct Storage<IMEX_F32> {
         return __ldg(p) - (float)weight(a);
     }
     static __device__ __forceinline__ float load_plain(const float* p, int a) { return *p - (float)weight(a); }
+    static __device__ __forceinline__ float dev(float v, int a) { return v - (float)weight(a); }
     static __device__ __forceinline__ float store(float h, int a) { return (float)weight(a) + h; }
     static __device__ __forceinline__ double to_f64(float v, int) { return (double)v; }
     static __device__ __forceinline__ float from_f64(double f, int) { return __double2float_rn(f); }
@@ -133,6 +138,7 @@ struct Storage<IMEX_F16DEV> {
     static constexpr float kScale = 4096.0f;
     static __device__ __forceinline__ float load(const __half* p, int) { return __half2float(__ldg(p)); }
     static __device__ __forceinline__ float load_plain(const __half* p, int) { return __half2float(*p); }
+    static __device__ __forceinline__ float dev(__half v, int) { return __half2float(v); }
     static __device__ __forceinline__ __half store(float h, int) { return __float2half_rn(h); }
     static __device__ __forceinline__ double to_f64(__half v, int a)
     {
@@ -144,60 +150,100 @@ struct Storage<IMEX_F16DEV> {
     }
 };
 
+// Arithmetic of one float32 lane (float) or of two cells in lock step
+// (float2, the packed f32x2 instructions of the sm_100 family).  The packed
+// operations are two independent IEEE operations each, so a float2 lane
+// gives exactly the bits the float code gives for that cell.  The float
+// operations are the _rn intrinsics, which the compiler never contracts
+// into a fused multiply-add (as it may contract a * b + c), so every
+// product and sum rounds exactly where the code says.
+struct F1 {
+    using V = float;
+    static __device__ __forceinline__ V splat(float x) { return x; }
+    static __device__ __forceinline__ V add(V a, V b) { return __fadd_rn(a, b); }
+    static __device__ __forceinline__ V sub(V a, V b) { return __fsub_rn(a, b); }
+    static __device__ __forceinline__ V mul(V a, V b) { return __fmul_rn(a, b); }
+    static __device__ __forceinline__ V fma(V a, V b, V c) { return __fmaf_rn(a, b, c); }
+};
+struct F2 {
+    using V = float2;
+    static __device__ __forceinline__ V splat(float x) { return make_float2(x, x); }
+    static __device__ __forceinline__ V add(V a, V b) { return __fadd2_rn(a, b); }
+    // a - b rounded once: b * (-1) is exact, so the fused form rounds a - b
+    static __device__ __forceinline__ V sub(V a, V b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
+    static __device__ __forceinline__ V mul(V a, V b) { return __fmul2_rn(a, b); }
+    static __device__ __forceinline__ V fma(V a, V b, V c) { return __ffma2_rn(a, b, c); }
+};
+
 // float32 BGK collision of the deviations h = kScale (f - w) (see the file
-// header).  Moments and the relaxation are linear in h; only the quadratic
-// terms of the equilibrium carry 1 / kScale, folded into their constants.
-// kScale is a power of two, so every intermediate is exactly kScale^k times
-// the unscaled one and the result is exactly kScale times the unscaled
-// collision's: both storage formats run the same float32 arithmetic.
-template <int P>
-__device__ __forceinline__ void collide_dev_f32(float (&h)[kQ], const CollideF32& cp)
+// header), for one cell (A = F1) or two (A = F2).  Moments and the
+// relaxation are linear in h; only the quadratic terms of the equilibrium
+// carry 1 / kScale, folded into their constants.  kScale is a power of two,
+// so every intermediate is exactly kScale^k times the unscaled one and the
+// result is exactly kScale times the unscaled collision's: both storage
+// formats run the same float32 arithmetic.  2 heq - h is formed as
+// (heq + heq) - h: heq + heq is exact, so it rounds like fma(2, heq, -h).
+template <int P, class A>
+__device__ __forceinline__ void collide_dev(typename A::V (&h)[kQ], const CollideF32& cp)
 {
+    using V = typename A::V;
     constexpr float c15 = -1.5f / Storage<P>::kScale, c45 = 4.5f / Storage<P>::kScale;
-    float d[kPairs + 1], s[kPairs + 1];
+    V d[kPairs + 1], s[kPairs + 1];
 #pragma unroll
     for (int k = 1; k <= kPairs; ++k) {
-        d[k] = h[2 * k - 1] - h[2 * k];
-        s[k] = h[2 * k - 1] + h[2 * k];
+        d[k] = A::sub(h[2 * k - 1], h[2 * k]);
+        s[k] = A::add(h[2 * k - 1], h[2 * k]);
     }
-    const float sig = ((((s[1] + s[2]) + (s[3] + s[4])) + ((s[5] + s[6]) + (s[7] + s[8]))) +
-                       (((s[9] + s[10]) + (s[11] + s[12])) + (s[13] + h[0])));
-    float u[3] = {0.f, 0.f, 0.f};
+    const V sig = A::add(A::add(A::add(A::add(s[1], s[2]), A::add(s[3], s[4])), A::add(A::add(s[5], s[6]), A::add(s[7], s[8]))),
+                         A::add(A::add(A::add(s[9], s[10]), A::add(s[11], s[12])), A::add(s[13], h[0])));
+    V u[3];
 #pragma unroll
-    for (int dim = 0; dim < 3; ++dim)
+    for (int dim = 0; dim < 3; ++dim) {
+        bool first = true;
 #pragma unroll
         for (int k = 1; k <= kPairs; ++k) {
             const int e = ex(2 * k - 1, dim);
-            if (e == 1) u[dim] += d[k];
-            if (e == -1) u[dim] -= d[k];
+            if (e == 0) continue;
+            // 0 + d and 0 - d are exact: the first term starts the sum
+            if (first) u[dim] = e == 1 ? d[k] : A::sub(A::splat(0.f), d[k]);
+            else u[dim] = e == 1 ? A::add(u[dim], d[k]) : A::sub(u[dim], d[k]);
+            first = false;
         }
-    const float udu = fmaf(u[2], u[2], fmaf(u[1], u[1], u[0] * u[0]));
-    const float base = fmaf(c15, udu, sig);
-    const float eps = cp.eps;
+    }
+    const V udu = A::fma(u[2], u[2], A::fma(u[1], u[1], A::mul(u[0], u[0])));
+    const V base = A::fma(A::splat(c15), udu, sig);
+    const V eps = A::splat(cp.eps);
     {
-        const float heq = cp.w[0] * base;
-        h[0] = fmaf(eps, h[0] - heq, fmaf(2.f, heq, -h[0]));
+        const V heq = A::mul(A::splat(cp.w[0]), base);
+        h[0] = A::fma(eps, A::sub(h[0], heq), A::sub(A::add(heq, heq), h[0]));
     }
 #pragma unroll
     for (int k = 1; k <= kPairs; ++k) {
         const int a = 2 * k - 1;
         const int cls = weight216(a) == 16 ? 1 : weight216(a) == 4 ? 2 : 3;
-        float edu = 0.f;
+        V edu;
         bool first = true;
 #pragma unroll
         for (int dim = 0; dim < 3; ++dim) {
             const int e = ex(a, dim);
             if (e != 0) {
-                edu = first ? (e == 1 ? u[dim] : -u[dim]) : (e == 1 ? edu + u[dim] : edu - u[dim]);
+                edu = first ? (e == 1 ? u[dim] : A::sub(A::splat(0.f), u[dim]))
+                            : (e == 1 ? A::add(edu, u[dim]) : A::sub(edu, u[dim]));
                 first = false;
             }
         }
-        const float A = cp.w[cls] * fmaf(c45 * edu, edu, base);
-        const float B = cp.w3[cls] * edu;
-        const float ep = A + B, em = A - B;
-        h[a] = fmaf(eps, h[a] - ep, fmaf(2.f, ep, -h[a]));
-        h[a + 1] = fmaf(eps, h[a + 1] - em, fmaf(2.f, em, -h[a + 1]));
+        const V Aq = A::mul(A::splat(cp.w[cls]), A::fma(A::mul(A::splat(c45), edu), edu, base));
+        const V Bq = A::mul(A::splat(cp.w3[cls]), edu);
+        const V ep = A::add(Aq, Bq), em = A::sub(Aq, Bq);
+        h[a] = A::fma(eps, A::sub(h[a], ep), A::sub(A::add(ep, ep), h[a]));
+        h[a + 1] = A::fma(eps, A::sub(h[a + 1], em), A::sub(A::add(em, em), h[a + 1]));
     }
+}
+
+template <int P>
+__device__ __forceinline__ void collide_dev_f32(float (&h)[kQ], const CollideF32& cp)
+{
+    collide_dev<P, F1>(h, cp);
 }
 
 }  // namespace lowp

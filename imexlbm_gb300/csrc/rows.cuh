@@ -153,6 +153,7 @@ struct RowConfig {
     int rows = 1;          // B: consecutive y-rows per stage (divides ny)
     int ctas_per_sm = 0;   // resident CTAs per SM (grid = SMs * this)
     int threads = 0;       // threads per CTA
+    int dir_bytes = 0;     // reduced precision: bytes per direction in a stage
 };
 
 template <class E>

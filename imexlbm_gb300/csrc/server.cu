@@ -81,6 +81,7 @@ struct imex_server {
     std::string fatal;  // first server-thread error (the thread then stops)
 
     std::vector<Active> active;  // server thread only
+    int64_t tuned_cells = 0;     // batch cells when the launch shapes were last tuned
     std::thread worker;
 
     double now() const { return std::chrono::duration<double>(Clock::now() - t0).count(); }
@@ -180,8 +181,19 @@ void serve(imex_server* s)
         }
         // one tick of the batch; admissions overlap it
         const auto t_tick = Clock::now();
-        int64_t before = 0;
-        for (const Active& a : s->active) before += imex_steps_done(a.h) * (int64_t)a.req.nx * a.req.ny * a.req.nz;
+        int64_t before = 0, cells = 0;
+        for (const Active& a : s->active) {
+            const int64_t c = (int64_t)a.req.nx * a.req.ny * a.req.nz;
+            before += imex_steps_done(a.h) * c;
+            cells += c;
+        }
+        // The launch shapes were tuned for the batch as it was; when its
+        // size has changed by more than 2x, let the batch tune them again.
+        if (cells > 2 * s->tuned_cells || 2 * cells < s->tuned_cells) {
+            imex_batch_set_launch(s->batch, 0, 0, 0);
+            imex_batch_set_row_launch(s->batch, 0, 0, 0, 1);
+            s->tuned_cells = cells;
+        }
         int rc = imex_batch_step(s->batch, s->steps_per_tick);
         if (!rc) admit(s, incoming);
         if (!rc) rc = imex_batch_synchronize(s->batch);

@@ -254,12 +254,15 @@ class Batch:
         self._check(self._L.imex_batch_get_launch(self._b, out))
         return tuple(out)
 
-    def set_row_launch(self, stages: int, stage_kb: int = 32, ctas_per_sm: int = 1) -> None:
-        """Row-staged kernel shape; stages 0 autotunes, -1 turns it off."""
-        self._check(self._L.imex_batch_set_row_launch(self._b, int(stages), int(stage_kb), int(ctas_per_sm)))
+    def set_row_launch(self, stages: int, dir_kb: int = 2, ctas_per_sm: int = 1, float32_members: bool = True) -> None:
+        """Row-staged kernel shape (stages, KiB per direction in a stage,
+        CTAs per SM, float32 members in it); stages 0 autotunes, -1 turns
+        the row kernel off."""
+        self._check(self._L.imex_batch_set_row_launch(self._b, int(stages), int(dir_kb), int(ctas_per_sm),
+                                                      int(bool(float32_members))))
 
     def get_row_launch(self):
-        out = (ctypes.c_int * 3)()
+        out = (ctypes.c_int * 4)()
         self._check(self._L.imex_batch_get_row_launch(self._b, out))
         return tuple(out)
 

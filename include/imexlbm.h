@@ -304,15 +304,17 @@ int imex_batch_set_launch(imex_batch *b, int threads, int cells_per_thread, int 
 int imex_batch_get_launch(imex_batch *b, int out[3]);
 
 /* Launch shape of the row-staged batch kernel, which takes the members
- * whose z-rows are a multiple of 16 bytes (nz * element size): ring depth
- * `stages`, stage size `stage_kb` KiB (a member's work item is the largest
- * block of y-rows whose 27 source runs fit one stage) and resident CTAs
- * per SM.  stages 0 autotunes (default); -1 turns the row kernel off, so
- * every member runs in the cell kernel.  imex_batch_get_row_launch gives
- * {stages, stage_kb, ctas_per_sm} (-1 when the tuner found the cell
- * kernel faster). */
-int imex_batch_set_row_launch(imex_batch *b, int stages, int stage_kb, int ctas_per_sm);
-int imex_batch_get_row_launch(imex_batch *b, int out[3]);
+ * whose z-rows are a multiple of 16 bytes (nz * element size) and at most
+ * dir_kb KiB: ring depth `stages`, `dir_kb` KiB per direction in a stage
+ * (1, 2 or 4; a member's work item is the largest block of y-rows that
+ * fits), resident CTAs per SM, and whether float32 members join it
+ * (float32_members != 0) or stay in the cell kernel.  stages 0 autotunes
+ * (default); -1 turns the row kernel off, so every member runs in the cell
+ * kernel.  imex_batch_get_row_launch gives {stages, dir_kb, ctas_per_sm,
+ * float32_members} (stages -1 when the tuner found the cell kernel
+ * faster). */
+int imex_batch_set_row_launch(imex_batch *b, int stages, int dir_kb, int ctas_per_sm, int float32_members);
+int imex_batch_get_row_launch(imex_batch *b, int out[4]);
 
 /* Steps per captured CUDA graph (default 16; 0 launches each step
  * directly). */

@@ -78,7 +78,8 @@ ROW_SPECS = SPECS + [  # rows of a multiple of 16 bytes: the row-staged kernel t
 ]
 
 
-@pytest.mark.parametrize("row_shape", [(-1, 0, 0), (2, 32, 1), (3, 16, 2), (4, 4, 1), (2, 100, 1)])
+@pytest.mark.parametrize("row_shape", [(-1, 0, 0, 1), (2, 1, 2, 1), (2, 2, 2, 1), (2, 2, 2, 0), (3, 1, 1, 1),
+                                       (2, 4, 1, 0), (4, 2, 1, 1)])
 @pytest.mark.parametrize("graph", [0, 6])
 def test_row_kernel_equals_alone(imex, row_shape, graph):
     """The row-staged batch kernel (and the cell kernel beside it for the
@@ -105,7 +106,7 @@ def test_row_kernel_member_limits(imex):
     limits = [3, 11, -1, 7]
     lats = [make(imex, s) for s in specs]
     with imex.Batch(8) as b:
-        b.set_row_launch(2, 32, 1)
+        b.set_row_launch(2, 1, 2)
         b.set_graph(5)
         for lat, lim in zip(lats, limits):
             b.add(lat, lim)
@@ -120,9 +121,11 @@ def test_row_kernel_member_limits(imex):
 def test_row_launch_checks(imex):
     with imex.Batch(2) as b:
         with pytest.raises(imex.ImexError):
-            b.set_row_launch(2, 200, 2)       # two CTAs' rings exceed an SM
+            b.set_row_launch(3, 2, 2)         # two CTAs' rings exceed an SM
         with pytest.raises(imex.ImexError):
-            b.set_row_launch(1, 32, 1)        # one stage cannot overlap
+            b.set_row_launch(2, 3, 1)         # 1 or 2 KiB per direction
+        with pytest.raises(imex.ImexError):
+            b.set_row_launch(1, 1, 1)         # one stage cannot overlap
 
 
 def test_members_join_leave_and_finish(imex):
