@@ -149,10 +149,14 @@ __global__ void __launch_bounds__(256) k_batch(const BatchHeader* __restrict__ h
 template <int kDirBytes>
 __global__ void __launch_bounds__(rowslp::kThreads, 2)
     k_batch_rows(const RowsHeader* __restrict__ hdr, const BatchEntry* __restrict__ tab, int s, CollideF32 base,
-                 int stages, unsigned* __restrict__ err)
+                 int stages, int table_cap, unsigned* __restrict__ err)
 {
     extern __shared__ __align__(128) unsigned char smem[];
     const int count = hdr->count;
+    if (count > table_cap) {  // the table would not fit the shared memory the launch has
+        if (threadIdx.x == 0) atomicOr(err, 2u);
+        return;
+    }
     const unsigned total = hdr->total;
     unsigned* sbegin = reinterpret_cast<unsigned*>(smem + rowslp::smem_bytes(kDirBytes, stages));
     for (int q = threadIdx.x; q < count; q += blockDim.x) sbegin[q] = tab[q].ibegin;
@@ -267,7 +271,8 @@ CollideF32 base_constants()
 }
 
 // Shared memory of a row-kernel CTA: barriers, ring and the table of the
-// members' first items.
+// members' first items, sized for the batch's capacity - a CUDA graph keeps
+// the size it was captured with while members join.
 size_t rows_smem(const RowShape& rs, int members)
 {
     return rowslp::smem_bytes(rs.dir_kb * 1024, rs.stages) + ((sizeof(unsigned) * (members + 1) + 15) & ~15ull);
@@ -302,20 +307,20 @@ cudaError_t launch_step(imex_batch* b, const BatchShape& sh, const RowShape& rs,
         const unsigned items = b->h_rhdr->total;
         unsigned grid = (unsigned)(b->sms * rs.ctas_per_sm);
         if (grid > items) grid = items;
-        if (!rows_fit(rs, b->n_row)) return cudaErrorInvalidValue;
-        const size_t smem = rows_smem(rs, b->n_row);
+        if (!rows_fit(rs, b->capacity)) return cudaErrorInvalidValue;
+        const size_t smem = rows_smem(rs, b->capacity);
         switch (rs.dir_kb) {
         case 1:
             k_batch_rows<1024><<<grid, rowslp::kThreads, smem, b->stream>>>(b->d_rhdr, b->d_rtab, s, base, rs.stages,
-                                                                            b->d_err);
+                                                                            b->capacity, b->d_err);
             break;
         case 2:
             k_batch_rows<2048><<<grid, rowslp::kThreads, smem, b->stream>>>(b->d_rhdr, b->d_rtab, s, base, rs.stages,
-                                                                            b->d_err);
+                                                                            b->capacity, b->d_err);
             break;
         case 4:
             k_batch_rows<4096><<<grid, rowslp::kThreads, smem, b->stream>>>(b->d_rhdr, b->d_rtab, s, base, rs.stages,
-                                                                            b->d_err);
+                                                                            b->capacity, b->d_err);
             break;
         default: return cudaErrorInvalidValue;
         }
@@ -508,7 +513,7 @@ int tune_batch(imex_batch* b, bool tune_cells, bool tune_rows)
         if (rc) return rc;
         RowShape best_rs = off;
         for (RowShape rs : row_candidates()) {
-            if (!rows_fit(rs, (int)b->members.size())) continue;
+            if (!rows_fit(rs, b->capacity)) continue;
             for (int f32 = 1; f32 >= 0; --f32) {
                 rs.f32 = f32;
                 float ms = 0.f;
@@ -714,8 +719,10 @@ int imex_batch_synchronize(imex_batch* b)
     B_CUDA(b, cudaStreamSynchronize(b->stream), "imex_batch_synchronize");
     if (v) {
         B_CUDA(b, cudaMemset(b->d_err, 0, sizeof v), "cudaMemset");
-        return bfail(b, IMEX_ERR_CUDA, "imex_batch_synchronize: a row kernel's asynchronous copy did not complete in "
-                                       "time; the members' results are invalid");
+        return bfail(b, IMEX_ERR_CUDA, (v & 2u) ? "imex_batch_synchronize: the row kernel's member table exceeded "
+                                                  "its shared memory; the members' results are invalid"
+                                                : "imex_batch_synchronize: a row kernel's asynchronous copy did not "
+                                                  "complete in time; the members' results are invalid");
     }
     return IMEX_OK;
 }

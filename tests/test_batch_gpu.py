@@ -118,6 +118,27 @@ def test_row_kernel_member_limits(imex):
         lat.close()
 
 
+def test_row_kernel_graph_while_members_join(imex):
+    """A captured graph stays in use while row-kernel members join: the
+    member table must fit the launch's shared memory whatever the count."""
+    specs = ROW_SPECS[6:] + [SPECS[0], SPECS[2], SPECS[4]]
+    lats = [make(imex, s) for s in specs]
+    joined_at = [0, 0, 4, 8, 8, 12, 16]
+    with imex.Batch(16) as b:
+        b.set_row_launch(2, 2, 2)
+        b.set_graph(4)
+        for t in range(0, 20, 4):
+            for lat, j in zip(lats, joined_at):
+                if j == t:
+                    b.add(lat)
+            b.step(4)
+        b.synchronize()
+    for lat, spec, j in zip(lats, specs, joined_at):
+        assert lat.steps_done() == 20 - j
+        assert np.array_equal(lat.get_f(), alone(imex, spec, 20 - j))
+        lat.close()
+
+
 def test_row_launch_checks(imex):
     with imex.Batch(2) as b:
         with pytest.raises(imex.ImexError):
