@@ -50,7 +50,7 @@ def tau_of(edge, re, u0):
     return System(text=f"1.0 0.1 {re}\n{u0} 1 1\n{edge} {edge} {edge}\n").tau
 
 
-def run(n=64, steps=500, precision="f32", seed=20261203, log=print, check_fp64=True, row_launch=None):
+def run(n=64, steps=500, precision="f32", seed=20261203, log=print, check_fp64=True, row_launch=None, launch=None):
     import torch
 
     work = workload(n, seed, precision)
@@ -65,6 +65,8 @@ def run(n=64, steps=500, precision="f32", seed=20261203, log=print, check_fp64=T
     batch = Batch(max(2, n))
     if row_launch is not None:
         batch.set_row_launch(*row_launch)
+    if launch is not None:
+        batch.set_launch(*launch)
     for lat in lats:
         batch.add(lat)
     m0 = [lat.Conserved()[0] for lat in lats]
@@ -121,10 +123,13 @@ def main(argv=None) -> int:
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--row-launch", default=None, metavar="STAGES,KB,CTAS",
                     help="pin the row kernel's shape (-1,0,0: off) instead of autotuning it")
+    ap.add_argument("--launch", default=None, metavar="THREADS,CPT,CTAS",
+                    help="pin the one-thread-per-cell kernel's shape instead of autotuning it")
     ap.add_argument("--json", default=None)
     a = ap.parse_args(argv)
     rl = tuple(int(v) for v in a.row_launch.split(",")) if a.row_launch else None
-    r = run(a.lattices, a.steps, a.precision, a.seed, check_fp64=not a.no_fp64, row_launch=rl)
+    cl = tuple(int(v) for v in a.launch.split(",")) if a.launch else None
+    r = run(a.lattices, a.steps, a.precision, a.seed, check_fp64=not a.no_fp64, row_launch=rl, launch=cl)
     if a.json:
         with open(a.json, "w") as fp:
             json.dump(r, fp, indent=1)

@@ -199,11 +199,11 @@ int time_shape(imex_lattice* h, const RowConfig& rc, float* ms)
     IMEX_CUDA(h, cudaEventCreate(&e0), "cudaEventCreate");
     IMEX_CUDA(h, cudaEventCreate(&e1), "cudaEventCreate");
     cudaError_t e = cudaSuccess;
-    const int reps = 3;
+    const int reps = 5;
     float best = 0.f;
-    // one warm-up launch, then the faster of two timed rounds of `reps`
+    // one warm-up launch, then the fastest of three timed rounds of `reps`
     e = rc.stages > 0 ? launch_fused_rows(h, src, dst, rc) : launch_fused_classic(h, src, dst);
-    for (int round = 0; round < 2 && e == cudaSuccess; ++round) {
+    for (int round = 0; round < 3 && e == cudaSuccess; ++round) {
         e = cudaEventRecord(e0, h->stream);
         for (int r = 0; r < reps && e == cudaSuccess; ++r) {
             e = rc.stages > 0 ? launch_fused_rows(h, src, dst, rc) : launch_fused_classic(h, src, dst);

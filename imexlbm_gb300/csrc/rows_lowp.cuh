@@ -38,7 +38,8 @@ namespace imex {
 namespace rowslp {
 
 constexpr int kThreads = 256;
-constexpr int kBarBytes = 128;  // up to 16 mbarriers
+constexpr int kMaxStages = 16;
+constexpr int kBarBytes = 128;  // kMaxStages mbarriers
 
 // One work item.
 struct Item {
@@ -55,10 +56,13 @@ struct Item {
 
 __device__ __forceinline__ uint32_t elem_bytes(int prec) { return prec == IMEX_F32 ? 4u : 2u; }
 
-// Shared memory of a CTA: barriers and `stages` ring stages.
+// Descriptors of the items in the ring, one per stage (128-byte aligned).
+constexpr int kSlotBytes = (int)((kMaxStages * sizeof(Item) + 127) / 128 * 128);
+
+// Shared memory of a CTA: barriers, item descriptors and `stages` ring stages.
 __host__ __device__ inline size_t smem_bytes(int dir_bytes, int stages)
 {
-    return kBarBytes + (size_t)stages * kQ * dir_bytes;
+    return kBarBytes + kSlotBytes + (size_t)stages * kQ * dir_bytes;
 }
 
 // Collide the item staged at `in` into the lattice's destination buffer;
@@ -139,27 +143,33 @@ __device__ __forceinline__ void compute_item(const unsigned char* __restrict__ i
 }
 
 // The persistent loop of one CTA over its items t = 0 .. my-1 (item_of(t)
-// describes item t; every thread computes the same).  smem: kBarBytes of
-// mbarriers, then `stages` stages of 27 * kDirBytes.
+// describes item t).  smem: kBarBytes of mbarriers, a descriptor slot per
+// stage, then `stages` stages of 27 * kDirBytes.  Thread 0 describes each
+// item once, when it arms the item's stage, into the stage's slot; the
+// other threads read the slot (a member lookup per item per thread - a
+// binary search and a table read for a batch - would sit in front of every
+// item's loads and arithmetic).
 template <int kDirBytes, class Ar, class ItemOf>
 __device__ __forceinline__ void run_items(const ItemOf& item_of, int my, int stages, const CollideF32& base,
                                           unsigned char* smem, unsigned* __restrict__ err)
 {
     constexpr uint32_t kStage = (uint32_t)kQ * kDirBytes;
     uint64_t* full = reinterpret_cast<uint64_t*>(smem);
-    unsigned char* ring = smem + kBarBytes;
+    Item* slots = reinterpret_cast<Item*>(smem + kBarBytes);
+    unsigned char* ring = smem + kBarBytes + kSlotBytes;
     constexpr int nwarps = kThreads / 32;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int my_dir = warp + nwarps * lane;  // copies of direction my_dir are issued by this lane
     const bool issuer = my_dir < kQ;
 
-    auto arm = [&](int t) {
+    auto arm = [&](int t) {  // thread 0
         const Item it = item_of(t);
+        slots[t % stages] = it;
         const uint32_t bytes = it.active ? (uint32_t)kQ * it.B * it.nz * elem_bytes(it.prec) : 0u;
         bulk::mbar_arrive_expect_tx(&full[t % stages], bytes);
     };
-    auto issue = [&](int t) {
-        const Item it = item_of(t);
+    auto issue = [&](int t) {  // after the barrier that follows arm(t)
+        const Item it = slots[t % stages];
         if (!it.active) return;
         const uint32_t es = elem_bytes(it.prec);
         const uint32_t row_bytes = (uint32_t)it.nz * es;
@@ -191,8 +201,10 @@ __device__ __forceinline__ void run_items(const ItemOf& item_of, int my, int sta
         for (int t = 0; t < stages - 1 && t < my; ++t) issue(t);
 
     for (int t = 0; t < my; ++t) {
-        if (issuer && t + stages - 1 < my) issue(t + stages - 1);
         const int s = t % stages;
+        // read before the barrier below: thread 0 rewrites the slot after it
+        const Item it = slots[s];
+        if (issuer && t + stages - 1 < my) issue(t + stages - 1);
         const int ok = bulk::mbar_wait(&full[s], (uint32_t)((t / stages) & 1));
         if (__syncthreads_or(!ok)) {
             // A copy did not complete: record it, wait (bounded) for the
@@ -205,7 +217,6 @@ __device__ __forceinline__ void run_items(const ItemOf& item_of, int my, int sta
             __syncthreads();
             return;
         }
-        const Item it = item_of(t);
         if (it.active) {
             if (it.prec == IMEX_F32) compute_item<IMEX_F32, kDirBytes, Ar>(ring + (size_t)s * kStage, it, base);
             else compute_item<IMEX_F16DEV, kDirBytes, Ar>(ring + (size_t)s * kStage, it, base);
