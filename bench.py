@@ -139,6 +139,25 @@ def dist_env():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
 
 
+def max_over_ranks(x: float, world: int) -> float:
+    """The largest x over the ranks (the job's time is its slowest rank's);
+    x itself on one rank.  Works on any process-group backend."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_mlups(cells: int, steps: int, world: int, seconds: float) -> float:
+    """Whole-job throughput: every rank advances its own `cells` lattice
+    `steps` steps (replicas), in the slowest rank's `seconds`."""
+    return cells * steps * world / seconds / 1e6
+
+
 # -------------------------------------------------------------- CPU timing --
 def time_cpu_oracle(n: int, tau: float, steps: int, warmup: int, budget_s: float):
     """Time the oracle on an n x n x nz slab with nz chosen so that
@@ -276,13 +295,8 @@ def run_ours(a):
     gpu_launches = lat.kernel_launches() - launches0
     ms = ev0.elapsed_time(ev1)
     fallback = lat.fallback_cells(reset=True)
-    t_max = ms
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_max = float(t.item())
-    value = cells * a.steps * world / (t_max * 1e-3) / 1e6
+    t_max = max_over_ranks(ms, world)
+    value = job_mlups(cells, a.steps, world, t_max * 1e-3)
     cons = lat.Conserved()
 
     # roofline of the fused step kernel: every timed launch is that kernel
@@ -326,14 +340,9 @@ def run_ours(a):
                 lat2.Conserved()
                 reports += 1
         m._lib.check(L.imex_get_f(lat2.handle, dp, nval), lat2.handle)
-        dt = time.perf_counter() - t0
-        if world > 1:
-            import torch.distributed as dist
-            t = torch.tensor([dt], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            dt = float(t.item())
+        dt = max_over_ranks(time.perf_counter() - t0, world)
         lat2.close()
-        e2e = {"value": round(cells * a.steps * world / dt / 1e6, 2), "unit": "MLUPS",
+        e2e = {"value": round(job_mlups(cells, a.steps, world, dt), 2), "unit": "MLUPS",
                "h2d_bytes_per_step": round(nval * 8 / a.steps, 1),
                "d2h_bytes_per_step": round((nval * 8 + 40 * reports) / a.steps, 1),
                "what": f"imex_set_f from pinned host, {a.steps} steps with imex_conserved every "

@@ -193,7 +193,7 @@ __global__ void __launch_bounds__(rowslp::kThreads, 2)
         it.active = s < e.steps;
         return it;
     };
-    rowslp::run_items<kDirBytes, lowp::F2>(item_of, my, stages, base, smem, err);
+    rowslp::run_items<kDirBytes, lowp::F2, true>(item_of, my, stages, base, smem, err);
 }
 
 }  // namespace

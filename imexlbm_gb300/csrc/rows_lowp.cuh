@@ -56,8 +56,10 @@ struct Item {
 
 __device__ __forceinline__ uint32_t elem_bytes(int prec) { return prec == IMEX_F32 ? 4u : 2u; }
 
-// Descriptors of the items in the ring, one per stage (128-byte aligned).
-constexpr int kSlotBytes = (int)((kMaxStages * sizeof(Item) + 127) / 128 * 128);
+// Descriptors of the items in flight: one slot more than the stages, so
+// that an item's slot is rewritten only after every thread has finished
+// the item (128-byte aligned).
+constexpr int kSlotBytes = (int)(((kMaxStages + 1) * sizeof(Item) + 127) / 128 * 128);
 
 // Shared memory of a CTA: barriers, item descriptors and `stages` ring stages.
 __host__ __device__ inline size_t smem_bytes(int dir_bytes, int stages)
@@ -143,13 +145,17 @@ __device__ __forceinline__ void compute_item(const unsigned char* __restrict__ i
 }
 
 // The persistent loop of one CTA over its items t = 0 .. my-1 (item_of(t)
-// describes item t).  smem: kBarBytes of mbarriers, a descriptor slot per
-// stage, then `stages` stages of 27 * kDirBytes.  Thread 0 describes each
-// item once, when it arms the item's stage, into the stage's slot; the
-// other threads read the slot (a member lookup per item per thread - a
+// describes item t).  smem: kBarBytes of mbarriers, stages + 1 descriptor
+// slots, then `stages` stages of 27 * kDirBytes.  Thread 0 describes each
+// item once, when it arms the item's stage, into slot t % (stages + 1);
+// the other threads read the slot (a member lookup per item per thread - a
 // binary search and a table read for a batch - would sit in front of every
-// item's loads and arithmetic).
-template <int kDirBytes, class Ar, class ItemOf>
+// item's loads and arithmetic).  Slot t is rewritten by arm(t + stages + 1)
+// at the end of iteration t + 1, after the barrier that ends item t.
+//
+// kSlots false: every thread describes the items itself (one lattice: a
+// division, cheaper than the shared-memory reads).
+template <int kDirBytes, class Ar, bool kSlots, class ItemOf>
 __device__ __forceinline__ void run_items(const ItemOf& item_of, int my, int stages, const CollideF32& base,
                                           unsigned char* smem, unsigned* __restrict__ err)
 {
@@ -162,14 +168,15 @@ __device__ __forceinline__ void run_items(const ItemOf& item_of, int my, int sta
     const int my_dir = warp + nwarps * lane;  // copies of direction my_dir are issued by this lane
     const bool issuer = my_dir < kQ;
 
+    const int nslots = stages + 1;
     auto arm = [&](int t) {  // thread 0
         const Item it = item_of(t);
-        slots[t % stages] = it;
+        if (kSlots) slots[t % nslots] = it;
         const uint32_t bytes = it.active ? (uint32_t)kQ * it.B * it.nz * elem_bytes(it.prec) : 0u;
         bulk::mbar_arrive_expect_tx(&full[t % stages], bytes);
     };
     auto issue = [&](int t) {  // after the barrier that follows arm(t)
-        const Item it = slots[t % stages];
+        const Item it = kSlots ? slots[t % nslots] : item_of(t);
         if (!it.active) return;
         const uint32_t es = elem_bytes(it.prec);
         const uint32_t row_bytes = (uint32_t)it.nz * es;
@@ -202,8 +209,6 @@ __device__ __forceinline__ void run_items(const ItemOf& item_of, int my, int sta
 
     for (int t = 0; t < my; ++t) {
         const int s = t % stages;
-        // read before the barrier below: thread 0 rewrites the slot after it
-        const Item it = slots[s];
         if (issuer && t + stages - 1 < my) issue(t + stages - 1);
         const int ok = bulk::mbar_wait(&full[s], (uint32_t)((t / stages) & 1));
         if (__syncthreads_or(!ok)) {
@@ -217,6 +222,7 @@ __device__ __forceinline__ void run_items(const ItemOf& item_of, int my, int sta
             __syncthreads();
             return;
         }
+        const Item& it = kSlots ? slots[t % nslots] : item_of(t);
         if (it.active) {
             if (it.prec == IMEX_F32) compute_item<IMEX_F32, kDirBytes, Ar>(ring + (size_t)s * kStage, it, base);
             else compute_item<IMEX_F16DEV, kDirBytes, Ar>(ring + (size_t)s * kStage, it, base);
@@ -256,7 +262,7 @@ __global__ void __launch_bounds__(kThreads, 2)
         it.active = true;
         return it;
     };
-    run_items<kDirBytes, Ar>(item_of, my, stages, cp, smem, err);
+    run_items<kDirBytes, Ar, false>(item_of, my, stages, cp, smem, err);
 }
 
 }  // namespace rowslp

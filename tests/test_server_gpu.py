@@ -89,3 +89,23 @@ def test_bad_requests_refused(imex):
             srv.submit(256, 256, 256, 0.01, 0.05, 5, imex.IMEX_F32)  # larger than the budget
         with pytest.raises(imex.ImexError):
             srv.submit(0, 8, 8, 0.01, 0.05, 5, imex.IMEX_F32)
+
+
+def test_diverging_request_reports_nonfinite(imex):
+    """A solve that blows up (BGK at tau near 0 on a coarse grid at Mach 0.3)
+    still runs its steps and returns its diagnostics with IMEX_ERR_NONFINITE;
+    the server and the other requests carry on."""
+    with imex.Server(budget_bytes=1e9, max_active=4, steps_per_tick=10) as srv:
+        srv.submit(16, 16, 16, 1e-5, 0.3, 400, imex.IMEX_F32, tag=1)
+        srv.submit(16, 16, 16, 0.01, 0.05, 30, imex.IMEX_F32, tag=2)
+        got = {}
+        t0 = time.time()
+        while len(got) < 2 and time.time() - t0 < 60:
+            for r in srv.poll():
+                got[r["tag"]] = r
+            time.sleep(0.01)
+        assert srv.stats()["failed"] == 0
+    assert got[1]["status"] == imex.IMEX_ERR_NONFINITE
+    assert not np.all(np.isfinite(got[1]["conserved"]))
+    assert got[1]["steps"] == 400
+    assert got[2]["status"] == 0
