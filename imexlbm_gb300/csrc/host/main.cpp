@@ -178,6 +178,10 @@ int main(int argc, char* argv[])
             throw imex::Error(IMEX_ERR_ARG, imex_last_error(l1.handle()));
         std::printf("rx=%d,ry=%d,rz=%d\n", 1, 1, 1);  // setup_Cartesian on one rank
         l1.Initialize();
+        // choose the fused step's launch shape now (the autotuner times the
+        // candidates on this lattice) rather than inside the first timed steps
+        int shape[4];
+        if (imex_get_launch(l1.handle(), shape) != IMEX_OK) throw imex::Error(IMEX_ERR_CUDA, imex_last_error(l1.handle()));
         l1.fence();
         if (profile) l1.profile_enable(true);
         HostPhase p_step;

@@ -138,10 +138,88 @@ cudaError_t launch_step_fx(int mode, const double* src, double* dst, const Geom&
     return cudaGetLastError();
 }
 
+namespace {
+
+// Partial sums of {mass, px, py, pz, ke} (src/lbm.cpp:271-294), one partial
+// per block.  A cell's 27 values are summed exactly as 64-bit fixed point
+// (the collision's moments, fx_math.cuh) and each moment is rounded once to
+// float64; a cell outside the exact range sums in float64 as the reference
+// does.  Per-value float64 additions (~60 a cell on a float64 pipe of 1.67
+// operations per clock per SM) made this reduction 3.7 ms at 256^3, three
+// steps' worth.
+template <bool PULL>
+__global__ void __launch_bounds__(kStepBlock) k_conserved_fx(const double* __restrict__ src, Geom g,
+                                                             double* __restrict__ partial)
+{
+    __shared__ double smem[32 * 5];
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y, i = blockIdx.z;
+    double v[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    if (k < g.nz) {
+        const PullIndex pi(g, i, j, k, PULL);
+        double f[kQ];
+        gather27<double>(src, g, pi, f);
+        bool ok = true;
+        uint64_t X[kQ];
+#pragma unroll
+        for (int a = 0; a < kQ; ++a) X[a] = fx::to_fixed(f[a], a == 0 ? 8u : 5u, ok);
+        double pl, ul, vl, wl;
+        if (ok) {  // f_0 < 1, others < 1/8: every unsigned sum below 2^64
+            uint64_t S = 0, P[3] = {0, 0, 0}, M[3] = {0, 0, 0};
+#pragma unroll
+            for (int a = 0; a < kQ; ++a) {
+                S += X[a];
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                    if (ex(a, d) == 1) P[d] += X[a];
+                    if (ex(a, d) == -1) M[d] += X[a];
+                }
+            }
+            constexpr double scale = 1.0 / (double)(1ull << fx::kFrac);
+            pl = __ull2double_rn(S) * scale;
+            ul = __ll2double_rn((long long)(P[0] - M[0])) * scale;
+            vl = __ll2double_rn((long long)(P[1] - M[1])) * scale;
+            wl = __ll2double_rn((long long)(P[2] - M[2])) * scale;
+        } else {
+            pl = ul = vl = wl = 0.0;
+#pragma unroll
+            for (int a = 0; a < kQ; ++a) {
+                pl += f[a];
+                if (ex(a, 0) == 1) ul += f[a];
+                if (ex(a, 0) == -1) ul -= f[a];
+                if (ex(a, 1) == 1) vl += f[a];
+                if (ex(a, 1) == -1) vl -= f[a];
+                if (ex(a, 2) == 1) wl += f[a];
+                if (ex(a, 2) == -1) wl -= f[a];
+            }
+        }
+        v[0] = pl;
+        v[1] = ul;
+        v[2] = vl;
+        v[3] = wl;
+        v[4] = 0.5 * (ul * ul + vl * vl + wl * wl);
+    }
+    block_sum<5>(v, smem);
+    if (threadIdx.x == 0) {
+        const size_t b = ((size_t)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+#pragma unroll
+        for (int q = 0; q < 5; ++q) partial[b * 5 + q] = v[q];
+    }
+}
+
+}  // namespace
+
 cudaError_t launch_conserved_fx(bool pull, const double* src, const Geom& g, const FxParams&, double* partial,
                                 double* out, cudaStream_t s)
 {
-    return launch_conserved_f64(pull, src, g, partial, out, s);
+    const dim3 grid((g.nz + kStepBlock - 1) / kStepBlock, g.ny, g.nx);
+    if (pull)
+        k_conserved_fx<true><<<grid, kStepBlock, 0, s>>>(src, g, partial);
+    else
+        k_conserved_fx<false><<<grid, kStepBlock, 0, s>>>(src, g, partial);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    return launch_reduce_partials(partial, conserved_partials(g), out, s);
 }
 
 }  // namespace imex
