@@ -66,7 +66,8 @@ class Request(ctypes.Structure):
     _fields_ = [("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nz", ctypes.c_int),
                 ("precision", ctypes.c_int), ("rounding", ctypes.c_int), ("pad", ctypes.c_int),
                 ("tau", ctypes.c_double), ("rho0", ctypes.c_double), ("u0", ctypes.c_double),
-                ("phase", ctypes.c_double * 3), ("steps", ctypes.c_int64), ("tag", ctypes.c_int64)]
+                ("phase", ctypes.c_double * 3), ("steps", ctypes.c_int64), ("tag", ctypes.c_int64),
+                ("resume_path", ctypes.c_char * 256), ("save_path", ctypes.c_char * 256)]
 
 
 class Result(ctypes.Structure):

@@ -9,7 +9,8 @@
 //      (creating its lattice and initialising it on its own stream, so the
 //      initialisation overlaps the tick), and
 //   3. waits for the tick and retires the requests that reached their step
-//      count: reads their diagnostics, publishes the result, frees their
+//      count: reads their diagnostics, saves their state if asked (a later
+//      request can resume from it), publishes the result, frees their
 //      memory and slot.
 // Requests therefore join and leave between ticks while the others keep
 // running: the batch is the set of requests in flight, not a queue drained
@@ -22,6 +23,7 @@
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
+#include <cstring>
 #include <deque>
 #include <mutex>
 #include <string>
@@ -115,7 +117,9 @@ void admit(imex_server* s, std::vector<Pending>& incoming)
         const imex_request& q = p.req;
         int rc = imex_create(q.nx, q.ny, q.nz, q.tau, q.rho0, q.u0, q.precision, &a.h);
         if (!rc && q.precision == IMEX_F16DEV) rc = imex_set_rounding(a.h, q.rounding);
-        if (!rc) rc = imex_initialize_phase(a.h, q.phase[0], q.phase[1], q.phase[2]);
+        if (!rc)
+            rc = q.resume_path[0] ? imex_checkpoint_load(a.h, q.resume_path)
+                                  : imex_initialize_phase(a.h, q.phase[0], q.phase[1], q.phase[2]);
         if (!rc) rc = imex_batch_add(s->batch, a.h, q.steps);
         if (rc) {
             publish(s, a, rc, nullptr);
@@ -140,8 +144,12 @@ int retire(imex_server* s)
             continue;
         }
         double cons[5];
-        int rc = imex_conserved(a.h, cons);
         int rc2 = imex_batch_remove(s->batch, a.h);
+        int rc = imex_conserved(a.h, cons);
+        if (a.req.save_path[0]) {
+            const int rs = imex_checkpoint_save(a.h, a.req.save_path);
+            if (rs && (!rc || rc == IMEX_ERR_NONFINITE)) rc = rs;
+        }
         publish(s, a, rc, cons);
         imex_destroy(a.h);
         {
@@ -262,6 +270,10 @@ int imex_server_create(size_t budget_bytes, int max_active, int steps_per_tick, 
 int imex_server_submit(imex_server* s, const imex_request* req, int64_t* id)
 {
     if (!s || !req) return imex::set_thread_error(IMEX_ERR_ARG, "imex_server_submit: null argument");
+    if (std::memchr(req->resume_path, 0, sizeof req->resume_path) == nullptr ||
+        std::memchr(req->save_path, 0, sizeof req->save_path) == nullptr)
+        return imex::set_thread_error(IMEX_ERR_ARG, "imex_server_submit: resume_path and save_path must be "
+                                                    "NUL-terminated within 256 bytes");
     if (req->nx < 1 || req->ny < 1 || req->nz < 1 || req->steps < 0 ||
         (req->precision != IMEX_F32 && req->precision != IMEX_F16DEV) ||
         (req->rounding != IMEX_ROUND_NEAREST && req->rounding != IMEX_ROUND_STOCHASTIC))

@@ -301,7 +301,11 @@ class Server:
         self._s = s
 
     def submit(self, nx: int, ny: int, nz: int, tau: float, u0: float, steps: int, precision: int = _lib.IMEX_F32,
-               rho0: float = 1.0, phase=(0.0, 0.0, 0.0), rounding: int | None = None, tag: int = 0) -> int:
+               rho0: float = 1.0, phase=(0.0, 0.0, 0.0), rounding: int | None = None, tag: int = 0,
+               resume_path: str = "", save_path: str = "") -> int:
+        """Queue a solve; returns its id.  resume_path starts it from a
+        checkpoint (its step count included), save_path keeps its final
+        state: a solve can be paused and resumed across requests."""
         r = _lib.Request()
         r.nx, r.ny, r.nz = int(nx), int(ny), int(nz)
         r.precision = int(precision)
@@ -312,6 +316,11 @@ class Server:
         for i in range(3):
             r.phase[i] = float(phase[i])
         r.steps, r.tag = int(steps), int(tag)
+        for name, val in (("resume_path", resume_path), ("save_path", save_path)):
+            b = str(val).encode()
+            if len(b) >= 256:
+                raise ValueError(f"{name} longer than 255 bytes")
+            setattr(r, name, b)
         rid = ctypes.c_int64()
         check(self._L.imex_server_submit(self._s, ctypes.byref(r), ctypes.byref(rid)))
         return int(rid.value)

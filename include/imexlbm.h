@@ -343,8 +343,13 @@ typedef struct imex_request {
     int pad;
     double tau, rho0, u0; /* as imex_create */
     double phase[3];      /* as imex_initialize_phase */
-    int64_t steps;        /* reference steps to run */
+    int64_t steps;        /* step count to reach (from 0, or from the resumed state) */
     int64_t tag;          /* caller's tag, returned in the result */
+    char resume_path[256]; /* "" or a checkpoint (imex_checkpoint_save) to start
+                              from instead of the Taylor-Green field: pause and
+                              resume of a served solve */
+    char save_path[256];   /* "" or a file the final state is saved to
+                              (imex_checkpoint_save) before the result is published */
 } imex_request;
 
 typedef struct imex_result {

@@ -109,3 +109,45 @@ def test_diverging_request_reports_nonfinite(imex):
     assert not np.all(np.isfinite(got[1]["conserved"]))
     assert got[1]["steps"] == 400
     assert got[2]["status"] == 0
+
+
+def test_pause_and_resume_across_requests(imex, tmp_path):
+    """A solve saved at step 30 and resumed by a later request to step 70
+    ends where a single 70-step solve ends, bit for bit (stochastic
+    rounding included: the saved step count seeds the random bits)."""
+    ck = str(tmp_path / "req.ckpt")
+    for pname in ("f32", "f16dev"):
+        p = prec(imex, pname)
+        with imex.Server(budget_bytes=1e9, max_active=4, steps_per_tick=8) as srv:
+            srv.submit(20, 16, 24, 0.003, 0.06, 30, p, tag=1, save_path=ck)
+            first = _wait(srv, 1)
+            srv.submit(20, 16, 24, 0.003, 0.06, 70, p, tag=2, resume_path=ck)
+            srv.submit(20, 16, 24, 0.003, 0.06, 70, p, tag=3)
+            rest = _wait(srv, 2)
+        assert first[1]["status"] == 0 and first[1]["steps"] == 30
+        assert rest[2]["status"] == 0 and rest[2]["steps"] == 70
+        assert rest[2]["conserved"] == rest[3]["conserved"]
+        with imex.LBM(20, 16, 24, 0.003, 1.0, 0.06, precision=p) as lat:
+            lat.checkpoint_load(ck)
+            assert lat.steps_done() == 30
+
+
+def test_resume_from_missing_file_fails_that_request(imex, tmp_path):
+    with imex.Server(budget_bytes=1e9, max_active=2, steps_per_tick=5) as srv:
+        srv.submit(8, 8, 8, 0.01, 0.05, 10, imex.IMEX_F32, tag=1, resume_path=str(tmp_path / "nope"))
+        srv.submit(8, 8, 8, 0.01, 0.05, 10, imex.IMEX_F32, tag=2)
+        got = _wait(srv, 2)
+        assert srv.stats()["failed"] == 0
+    assert got[1]["status"] == imex.IMEX_ERR_IO
+    assert got[2]["status"] == 0
+
+
+def _wait(srv, n, timeout=60):
+    got = {}
+    t0 = time.time()
+    while len(got) < n and time.time() - t0 < timeout:
+        for r in srv.poll():
+            got[r["tag"]] = r
+        time.sleep(0.01)
+    assert len(got) == n
+    return got
