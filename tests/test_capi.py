@@ -85,3 +85,77 @@ def test_create_without_gpu_fails_cleanly(imex):
     rc = L.imex_create(8, 8, 8, 0.1, 1.0, 0.05, 0, ctypes.byref(h))
     assert rc == 2 and not h.value
     assert L.imex_last_error(None)
+
+
+def test_null_and_range_checks_of_every_entry_point(imex):
+    """Host-side argument checks that run before any CUDA call."""
+    L = imex.load()
+    out = (ctypes.c_double * 8)()
+    assert L.imex_conserved(None, out) == 1
+    assert L.imex_minmax_uvwp(None, out) == 1
+    assert L.imex_write_tecplot(None, b"x.plt", 1) == 1
+    assert L.imex_checkpoint_save(None, b"x") == 1
+    assert L.imex_checkpoint_load(None, b"x") == 1
+    assert L.imex_profile_enable(None, 1) == 1
+    assert L.imex_set_launch(None, 2, 1, 1) == 1
+    assert L.imex_set_rounding(None, 0) == 1
+    assert L.imex_steps_done(None) == -1
+    b = ctypes.c_void_p()
+    assert L.imex_batch_create(0, ctypes.byref(b)) == 1
+    assert L.imex_batch_create(4096, ctypes.byref(b)) == 1
+    assert L.imex_batch_add(None, None, -1) == 1
+    assert L.imex_batch_step(None, 1) == 1
+    assert L.imex_batch_set_row_launch(None, 2, 1, 1, 1) == 1
+    s = ctypes.c_void_p()
+    assert L.imex_server_create(0, 4, 5, ctypes.byref(s)) == 1
+    assert L.imex_server_create(10**9, 0, 5, ctypes.byref(s)) == 1
+    assert L.imex_server_create(10**9, 4, 0, ctypes.byref(s)) == 1
+    assert L.imex_server_submit(None, None, None) == 1
+    n = ctypes.c_int()
+    assert L.imex_server_poll(None, None, 0, ctypes.byref(n)) == 1
+    assert L.imex_server_now(None) == -1.0
+    L.imex_server_destroy(None)
+    L.imex_batch_destroy(None)
+
+
+@pytest.mark.skipif(gpu_available(), reason="checks the no-GPU error path")
+def test_batch_and_server_without_gpu_fail_cleanly(imex):
+    L = imex.load()
+    b = ctypes.c_void_p()
+    assert L.imex_batch_create(4, ctypes.byref(b)) == 2 and not b.value
+    s = ctypes.c_void_p()
+    assert L.imex_server_create(10**9, 4, 5, ctypes.byref(s)) == 2 and not s.value
+    assert L.imex_last_error(None)
+
+
+def test_struct_layouts_match_header(imex, tmp_path):
+    """The ctypes mirrors of the ABI's structs have the header's sizes and
+    field offsets (compiled here from include/imexlbm.h with the C compiler) -
+    what a cgo / JNI binding must also lay out."""
+    import shutil
+    import subprocess
+    from imexlbm_gb300 import _lib
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    checks = {"imex_request": (_lib.Request, ["nx", "precision", "tau", "phase", "steps", "tag", "resume_path",
+                                              "save_path"]),
+              "imex_result": (_lib.Result, ["id", "status", "conserved", "steps", "t_done"]),
+              "imex_server_stats": (_lib.ServerStats, ["queued", "busy_seconds", "failed"]),
+              "imex_phase_stats": (_lib.PhaseStats, ["calls", "max_ms"]),
+              "imex_deck": (_lib.Deck, ["rho0", "Re", "sz", "tau"])}
+    src = ['#include <stdio.h>', '#include <stddef.h>', '#include "imexlbm.h"', "int main(void) {"]
+    for st, (_, fields) in checks.items():
+        src.append(f'printf("{st} %zu\\n", sizeof({st}));')
+        for f in fields:
+            src.append(f'printf("{st}.{f} %zu\\n", offsetof({st}, {f}));')
+    src.append("return 0; }")
+    (tmp_path / "layout.c").write_text("\n".join(src))
+    inc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+    subprocess.run([cc, "-I", inc, str(tmp_path / "layout.c"), "-o", str(tmp_path / "layout")], check=True)
+    out = dict(line.split() for line in subprocess.run([str(tmp_path / "layout")], capture_output=True, text=True,
+                                                       check=True).stdout.splitlines())
+    for st, (py, fields) in checks.items():
+        assert int(out[st]) == ctypes.sizeof(py), st
+        for f in fields:
+            assert int(out[f"{st}.{f}"]) == getattr(py, f).offset, (st, f)
