@@ -146,8 +146,8 @@ __global__ void __launch_bounds__(256) k_batch(const BatchHeader* __restrict__ h
 // Row-staged batched step (rows_lowp.cuh): work items of every member in
 // one persistent loop; an item's member is found by binary search over the
 // members' first-item indices, kept in shared memory after the ring.
-template <int kDirBytes>
-__global__ void __launch_bounds__(rowslp::kThreads, 2)
+template <int kDirBytes, int kMinBlocks>
+__global__ void __launch_bounds__(rowslp::kThreads, kMinBlocks)
     k_batch_rows(const RowsHeader* __restrict__ hdr, const BatchEntry* __restrict__ tab, int s, CollideF32 base,
                  int stages, int table_cap, unsigned* __restrict__ err)
 {
@@ -183,9 +183,10 @@ __global__ void __launch_bounds__(rowslp::kThreads, 2)
         it.nz = e.nz;
         it.B = e.B;
         const unsigned local = itx - sbegin[lo];
-        const unsigned yblocks = (unsigned)(e.ny / e.B);
+        const unsigned yblocks = (unsigned)rowslp::y_blocks(e.ny, e.B);
         it.x = (int)(local / yblocks);
         it.y0 = (int)(local - (unsigned)it.x * yblocks) * e.B;
+        if (e.ny - it.y0 < it.B) it.B = e.ny - it.y0;  // the last block of a plane may be shorter
         it.prec = e.prec;
         it.eps = e.eps;
         it.sr = e.sr;
@@ -309,21 +310,23 @@ cudaError_t launch_step(imex_batch* b, const BatchShape& sh, const RowShape& rs,
         if (grid > items) grid = items;
         if (!rows_fit(rs, b->capacity)) return cudaErrorInvalidValue;
         const size_t smem = rows_smem(rs, b->capacity);
+        const bool one = rs.ctas_per_sm <= 1;  // one resident CTA: the full register file
+#define IMEX_BATCH_ROWS(D, M) \
+    k_batch_rows<D, M><<<grid, rowslp::kThreads, smem, b->stream>>>(b->d_rhdr, b->d_rtab, s, base, rs.stages, \
+                                                                   b->capacity, b->d_err)
         switch (rs.dir_kb) {
         case 1:
-            k_batch_rows<1024><<<grid, rowslp::kThreads, smem, b->stream>>>(b->d_rhdr, b->d_rtab, s, base, rs.stages,
-                                                                            b->capacity, b->d_err);
+            if (one) IMEX_BATCH_ROWS(1024, 1);
+            else IMEX_BATCH_ROWS(1024, 2);
             break;
         case 2:
-            k_batch_rows<2048><<<grid, rowslp::kThreads, smem, b->stream>>>(b->d_rhdr, b->d_rtab, s, base, rs.stages,
-                                                                            b->capacity, b->d_err);
+            if (one) IMEX_BATCH_ROWS(2048, 1);
+            else IMEX_BATCH_ROWS(2048, 2);
             break;
-        case 4:
-            k_batch_rows<4096><<<grid, rowslp::kThreads, smem, b->stream>>>(b->d_rhdr, b->d_rtab, s, base, rs.stages,
-                                                                            b->capacity, b->d_err);
-            break;
+        case 4: IMEX_BATCH_ROWS(4096, 1); break;
         default: return cudaErrorInvalidValue;
         }
+#undef IMEX_BATCH_ROWS
         return cudaGetLastError();
     }
     return cudaSuccess;
@@ -337,9 +340,8 @@ int64_t owed(const imex_batch* b, size_t m, int64_t want)
     return left < 0 ? 0 : (left < want ? left : want);
 }
 
-// Rows per work item of a member in the row kernel under shape rs: the
-// largest divisor B of ny whose item (27 runs of B rows) fits a stage; 0 if
-// the member stays in the cell kernel.
+// Rows per work item of a member in the row kernel under shape rs
+// (rowslp::item_rows); 0 if the member stays in the cell kernel.
 int rows_per_item(const imex_lattice* h, const RowShape& rs)
 {
     if (rs.stages <= 0 || (h->precision == IMEX_F32 && !rs.f32)) return 0;
@@ -347,9 +349,7 @@ int rows_per_item(const imex_lattice* h, const RowShape& rs)
     const size_t cap = (size_t)rs.dir_kb * 1024;
     if (row_bytes % 16 || row_bytes > cap) return 0;
     if ((size_t)h->g.nx * h->g.ny >= 0x7fffffffu) return 0;
-    for (int B = (int)std::min<size_t>((size_t)h->g.ny, cap / row_bytes); B > 1; --B)
-        if (h->g.ny % B == 0) return B;
-    return 1;
+    return rowslp::item_rows(h->g.ny, h->g.nz, (int)lattice_elem_size(h->precision), (int)cap);
 }
 
 // Write the member tables for a tick where member m runs steps[m] fused
@@ -380,7 +380,7 @@ int upload_table(imex_batch* b, const std::vector<int>& steps, const RowShape& r
         if (B) {
             e.begin = 0;
             e.ibegin = ibegin;
-            ibegin += (unsigned)((size_t)h->g.nx * (h->g.ny / B));
+            ibegin += (unsigned)((size_t)h->g.nx * rowslp::y_blocks(h->g.ny, B));
         } else {
             e.begin = begin;
             e.ibegin = 0;
@@ -589,11 +589,15 @@ int imex_batch_create(int max_members, imex_batch** out)
     if (e == cudaSuccess) e = cudaMalloc(&b->d_err, sizeof(unsigned));
     if (e == cudaSuccess) e = cudaMemset(b->d_err, 0, sizeof(unsigned));
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_batch_rows<1024>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        e = cudaFuncSetAttribute(k_batch_rows<1024, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_batch_rows<2048>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        e = cudaFuncSetAttribute(k_batch_rows<1024, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_batch_rows<4096>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        e = cudaFuncSetAttribute(k_batch_rows<2048, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_batch_rows<2048, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_batch_rows<4096, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
     if (e != cudaSuccess) {
         imex_batch_destroy(b);
         cudaGetLastError();

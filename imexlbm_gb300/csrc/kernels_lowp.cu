@@ -2,6 +2,7 @@
 // float16 deviations 2^12 (f - w) (IMEX_F16DEV), collided in float32 by
 // lowp::collide_dev_f32 (lowp_math.cuh, which explains the arithmetic);
 // diagnostics accumulate in float64.
+#include <atomic>
 #include <cmath>
 
 #include <cuda_fp16.h>
@@ -242,14 +243,25 @@ bool rows_lowp_eligible(int prec, const Geom& g)
     return row % 16 == 0 && row <= (size_t)kRowsLowpDirMax && (size_t)g.nx * g.ny < 0x7fffffffu;
 }
 
-template <int D>
+template <int D, int MINB>
 cudaError_t launch_rows_lowp_d(int prec, const void* src, void* dst, const Geom& g, const CollideF32& cp,
                                const RowConfig& rc, unsigned* err, cudaStream_t s, unsigned grid)
 {
     const size_t smem = rowslp::smem_bytes(D, rc.stages);
-    cudaError_t e = cudaFuncSetAttribute(rowslp::k_rows_lowp<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    // raise the kernel's shared-memory limit once per device and size, not
+    // per launch (the attribute belongs to the device's context)
+    static std::atomic<int> allowed[64];
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
-    rowslp::k_rows_lowp<D><<<grid, rowslp::kThreads, smem, s>>>(src, dst, g, prec, rc.rows, cp, rc.stages, err);
+    if (dev >= 64 || (int)smem > allowed[dev].load()) {
+        e = cudaFuncSetAttribute(rowslp::k_rows_lowp<D, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem);
+        if (e != cudaSuccess) return e;
+        if (dev < 64) allowed[dev].store((int)smem);
+    }
+    rowslp::k_rows_lowp<D, MINB><<<grid, rowslp::kThreads, smem, s>>>(src, dst, g, prec, rc.rows, cp, rc.stages,
+                                                                       err);
     return cudaGetLastError();
 }
 
@@ -263,15 +275,20 @@ cudaError_t launch_rows_lowp(int prec, const void* src, void* dst, const Geom& g
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     }
     const size_t es = prec == IMEX_F32 ? 4 : 2;
-    if (rc.rows < 1 || g.ny % rc.rows || (size_t)rc.rows * g.nz * es > (size_t)rc.dir_bytes || rc.stages < 2)
+    if (rc.rows < 1 || (size_t)rc.rows * g.nz * es > (size_t)rc.dir_bytes || rc.stages < 2)
         return cudaErrorInvalidValue;
-    const long long items = (long long)g.nx * (g.ny / rc.rows);
+    const long long items = (long long)g.nx * rowslp::y_blocks(g.ny, rc.rows);
     long long grid = (long long)sms * rc.ctas_per_sm;
     if (grid > items) grid = items;
+    const bool one = rc.ctas_per_sm <= 1;  // one resident CTA: the full register file
     switch (rc.dir_bytes) {
-    case 1024: return launch_rows_lowp_d<1024>(prec, src, dst, g, cp, rc, err, s, (unsigned)grid);
-    case 2048: return launch_rows_lowp_d<2048>(prec, src, dst, g, cp, rc, err, s, (unsigned)grid);
-    case 4096: return launch_rows_lowp_d<4096>(prec, src, dst, g, cp, rc, err, s, (unsigned)grid);
+    case 1024:
+        return one ? launch_rows_lowp_d<1024, 1>(prec, src, dst, g, cp, rc, err, s, (unsigned)grid)
+                   : launch_rows_lowp_d<1024, 2>(prec, src, dst, g, cp, rc, err, s, (unsigned)grid);
+    case 2048:
+        return one ? launch_rows_lowp_d<2048, 1>(prec, src, dst, g, cp, rc, err, s, (unsigned)grid)
+                   : launch_rows_lowp_d<2048, 2>(prec, src, dst, g, cp, rc, err, s, (unsigned)grid);
+    case 4096: return launch_rows_lowp_d<4096, 1>(prec, src, dst, g, cp, rc, err, s, (unsigned)grid);
     default: return cudaErrorInvalidValue;
     }
 }

@@ -116,13 +116,12 @@ std::vector<RowConfig> row_candidates(const imex_lattice* h)
     std::vector<RowConfig> out;
     if (!rows_eligible_for(h)) return out;
     if (is_lowp(h)) {
-        // (stages, CTAs per SM) per direction block; B the most rows it holds
+        // (stages, CTAs per SM) per direction block; B from rowslp::item_rows
         const int shapes[][2] = {{2, 2}, {3, 2}, {2, 1}, {3, 1}, {4, 1}};
         const size_t row = (size_t)h->g.nz * elem_size(h->precision);
         for (int dir : {1024, 2048, 4096}) {
             if (row > (size_t)dir) continue;
-            int B = (int)std::min<size_t>((size_t)h->g.ny, dir / row);
-            while (h->g.ny % B) --B;
+            const int B = rowslp::item_rows(h->g.ny, h->g.nz, (int)elem_size(h->precision), dir);
             if (lowp_dir_bytes(h, B) != dir) continue;  // same items as a smaller block
             for (const auto& sh : shapes) {
                 const size_t smem = rowslp::smem_bytes(dir, sh[0]);
@@ -191,54 +190,52 @@ cudaError_t launch_fused_classic(imex_lattice* h, const void* src, void* dst)
 }
 
 // Time the fused step in shape rc (stages 0: classic); milliseconds per launch.
-int time_shape(imex_lattice* h, const RowConfig& rc, float* ms)
+// Milliseconds per launch of `reps` back-to-back fused steps in shape rc
+// (stages 0: classic).
+int time_shape(imex_lattice* h, const RowConfig& rc, int reps, float* ms)
 {
     const void* src = h->buf[h->cur];
     void* dst = h->buf[1 - h->cur];
     cudaEvent_t e0, e1;
     IMEX_CUDA(h, cudaEventCreate(&e0), "cudaEventCreate");
     IMEX_CUDA(h, cudaEventCreate(&e1), "cudaEventCreate");
-    cudaError_t e = cudaSuccess;
-    const int reps = 5;
-    float best = 0.f;
-    // one warm-up launch, then the fastest of three timed rounds of `reps`
-    e = rc.stages > 0 ? launch_fused_rows(h, src, dst, rc) : launch_fused_classic(h, src, dst);
-    for (int round = 0; round < 3 && e == cudaSuccess; ++round) {
-        e = cudaEventRecord(e0, h->stream);
-        for (int r = 0; r < reps && e == cudaSuccess; ++r) {
-            e = rc.stages > 0 ? launch_fused_rows(h, src, dst, rc) : launch_fused_classic(h, src, dst);
-            if (e == cudaSuccess) h->launches++;
-        }
-        if (e == cudaSuccess) e = cudaEventRecord(e1, h->stream);
-        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
-        float t = 0.f;
-        if (e == cudaSuccess) e = cudaEventElapsedTime(&t, e0, e1);
-        if (e == cudaSuccess && (round == 0 || t < best)) best = t;
+    cudaError_t e = cudaEventRecord(e0, h->stream);
+    for (int r = 0; r < reps && e == cudaSuccess; ++r) {
+        e = rc.stages > 0 ? launch_fused_rows(h, src, dst, rc) : launch_fused_classic(h, src, dst);
+        if (e == cudaSuccess) h->launches++;
     }
+    if (e == cudaSuccess) e = cudaEventRecord(e1, h->stream);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    float t = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&t, e0, e1);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (e != cudaSuccess) return cuda_fail(h, e, "autotune");
-    *ms = best / reps;
+    *ms = t / reps;
     return IMEX_OK;
 }
 
+// Time every candidate in interleaved rounds (so that a drift of the clock
+// or of the memory system during tuning does not favour one candidate) and
+// keep each candidate's fastest round; the fastest candidate wins.
 int tune(imex_lattice* h)
 {
     std::vector<RowConfig> cands = row_candidates(h);
     RowConfig best{};  // classic
     if (!cands.empty()) {
-        float best_ms = 0.f;
-        int rc = time_shape(h, best, &best_ms);
-        if (rc) return rc;
-        for (const RowConfig& c : cands) {
-            float ms = 0.f;
-            rc = time_shape(h, c, &ms);
-            if (rc) return rc;
-            if (ms < best_ms) {
-                best_ms = ms;
-                best = c;
+        cands.insert(cands.begin(), RowConfig{});
+        std::vector<float> fastest(cands.size(), 0.f);
+        for (int round = 0; round < 4; ++round)
+            for (size_t c = 0; c < cands.size(); ++c) {
+                float ms = 0.f;
+                int rc = time_shape(h, cands[c], round == 0 ? 1 : 4, &ms);  // round 0 warms up
+                if (rc) return rc;
+                if (round == 1 || ms < fastest[c]) fastest[c] = ms;
             }
-        }
+        size_t b = 0;
+        for (size_t c = 1; c < cands.size(); ++c)
+            if (fastest[c] < fastest[b]) b = c;
+        best = cands[b];
     }
     h->rows = best;
     std::lock_guard<std::mutex> guard(g_tune_lock);
@@ -769,7 +766,8 @@ int imex_set_launch(imex_lattice* h, int stages, int rows_per_stage, int ctas_pe
         return fail(h, IMEX_ERR_ARG, "imex_set_launch: the row-staged kernel needs nz*element size a multiple of 16 "
                                      "bytes and a fixed-point or reduced-precision engine");
     const int B = rows_per_stage < 1 ? 1 : rows_per_stage;
-    if (h->g.ny % B) return fail(h, IMEX_ERR_ARG, "imex_set_launch: rows_per_stage must divide ny");
+    if (!is_lowp(h) && h->g.ny % B) return fail(h, IMEX_ERR_ARG, "imex_set_launch: rows_per_stage must divide ny");
+    if (B > h->g.ny) return fail(h, IMEX_ERR_ARG, "imex_set_launch: rows_per_stage must not exceed ny");
     RowConfig rc;
     rc.stages = stages;
     rc.rows = B;

@@ -150,7 +150,7 @@ bool rows_eligible(const Geom& g)
 // Row-kernel launch shape.
 struct RowConfig {
     int stages = 0;        // ring depth (0: not the row kernel)
-    int rows = 1;          // B: consecutive y-rows per stage (divides ny)
+    int rows = 1;          // B: consecutive y-rows per stage (divides ny for float64)
     int ctas_per_sm = 0;   // resident CTAs per SM (grid = SMs * this)
     int threads = 0;       // threads per CTA
     int dir_bytes = 0;     // reduced precision: bytes per direction in a stage

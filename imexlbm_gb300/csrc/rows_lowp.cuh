@@ -24,7 +24,8 @@
 // same bits the one-cell kernels use.
 //
 // Requirements: nz * element size a multiple of 16 bytes (so nz is even and
-// every run is 16-byte aligned), B * nz * element size <= kDirBytes.
+// every run is 16-byte aligned), B * nz * element size <= kDirBytes.  B
+// need not divide ny: the last item of each x plane takes the rows left.
 #pragma once
 
 #include <cuda_fp16.h>
@@ -66,6 +67,39 @@ __host__ __device__ inline size_t smem_bytes(int dir_bytes, int stages)
 {
     return kBarBytes + kSlotBytes + (size_t)stages * kQ * dir_bytes;
 }
+
+// Rows per work item for a lattice of ny rows of nz cells of es bytes in a
+// stage with dir_bytes per direction: the B (B * nz * es <= dir_bytes) whose
+// items - ceil(ny / B) per x plane, the last one ny mod B rows when B does
+// not divide ny - keep the CTA's threads busiest, counting half a round of
+// kThreads pairs per item for its barrier and copies: the score
+// pairs / (sum over items of (rounds + 1/2) kThreads).  A 96-wide float16
+// lattice, for one, takes B = 10 in a 2 KB block (9 items of 480 pairs and
+// one of 288 per plane) rather than the largest divisor 8 (384 pairs, a half
+// idle second round).  0 if a single row does not fit.
+inline int item_rows(int ny, int nz, int es, int dir_bytes)
+{
+    const long long row = (long long)nz * es;
+    if (row > dir_bytes) return 0;
+    auto rounds = [](long long pairs) { return (pairs + kThreads - 1) / kThreads; };
+    const long long total = (long long)ny * nz / 2;
+    int best = 0;
+    double best_score = -1.0;
+    for (int B = 1; B <= ny && (long long)B * row <= dir_bytes; ++B) {
+        const int full = ny / B, last = ny % B;
+        double cost = full * (rounds((long long)B * nz / 2) + 0.5);
+        if (last) cost += rounds((long long)last * nz / 2) + 0.5;
+        const double score = (double)total / (cost * kThreads);
+        if (score >= best_score) {
+            best_score = score;
+            best = B;
+        }
+    }
+    return best;
+}
+
+// Number of y-blocks of a plane with items of B rows.
+__host__ __device__ inline int y_blocks(int ny, int B) { return (ny + B - 1) / B; }
 
 // Collide the item staged at `in` into the lattice's destination buffer;
 // Ar is the two-cell arithmetic (lowp::F2).
@@ -232,14 +266,16 @@ __device__ __forceinline__ void run_items(const ItemOf& item_of, int my, int sta
     }
 }
 
-// One lattice: items are the nx * ny / B row blocks in x-major order.
-template <int kDirBytes, class Ar = lowp::F2>
-__global__ void __launch_bounds__(kThreads, 2)
+// One lattice: items are the nx * ceil(ny / B) row blocks in x-major order.
+// kMinBlocks: resident CTAs per SM the register budget is cut for (1: up to
+// 255 registers; 2: 128).
+template <int kDirBytes, int kMinBlocks, class Ar = lowp::F2>
+__global__ void __launch_bounds__(kThreads, kMinBlocks)
     k_rows_lowp(const void* __restrict__ src, void* __restrict__ dst, Geom g, int prec, int B, CollideF32 cp,
                 int stages, unsigned* __restrict__ err)
 {
     extern __shared__ __align__(128) unsigned char smem[];
-    const int yblocks = g.ny / B;
+    const int yblocks = y_blocks(g.ny, B);
     const int items = g.nx * yblocks;
     const int G = gridDim.x;
     const int my = (int)blockIdx.x < items ? (items - 1 - (int)blockIdx.x) / G + 1 : 0;
@@ -252,9 +288,9 @@ __global__ void __launch_bounds__(kThreads, 2)
         it.nx = g.nx;
         it.ny = g.ny;
         it.nz = g.nz;
-        it.B = B;
         it.x = item / yblocks;
         it.y0 = (item - it.x * yblocks) * B;
+        it.B = g.ny - it.y0 < B ? g.ny - it.y0 : B;  // the last block of a plane may be shorter
         it.prec = prec;
         it.eps = cp.eps;
         it.sr = cp.sr;

@@ -213,7 +213,8 @@ int imex_conserved_noalloc(const double *f_dev, int nx, int ny, int nz, double *
 /* Launch shape of the fused step.  stages = 0: one thread per cell pulling
  * straight from global memory.  stages >= 2: the row-staged kernel - each
  * CTA keeps a ring of `stages` work items in shared memory, an item being
- * rows_per_stage consecutive y-rows (dividing ny) whose 27 source row runs
+ * rows_per_stage consecutive y-rows (dividing ny for float64; for reduced
+ * precision the last item of a plane takes the rows left) whose 27 source row runs
  * arrive by asynchronous bulk copies - with ctas_per_sm resident CTAs per
  * SM; it needs nz * element size a multiple of 16 bytes and the fixed-point
  * or a reduced-precision engine.  stages < 0: back to automatic.  By

@@ -37,8 +37,8 @@ def test_rows_bitwise_equal_classic(imex, shape, pname):
     for stages, rows, ctas in RING:
         try:
             got, c = run(imex, shape, prec, stages, rows, ctas)
-        except imex.ImexError as e:  # ring does not fit or rows do not divide ny
-            assert "shared memory" in str(e) or "divide" in str(e)
+        except imex.ImexError as e:  # ring does not fit, or rows do not divide / exceed ny
+            assert "shared memory" in str(e) or "divide" in str(e) or "exceed" in str(e)
             continue
         assert np.array_equal(got, ref), (shape, pname, stages, rows, ctas)
         assert c == cref
