@@ -472,7 +472,6 @@ int time_step(imex_batch* b, const BatchShape& sh, const RowShape& rs, float* ms
     B_CUDA(b, cudaEventCreate(&e0), "cudaEventCreate");
     B_CUDA(b, cudaEventCreate(&e1), "cudaEventCreate");
     cudaError_t e = launch_step(b, sh, rs, 0);  // warm-up
-    for (int r = 0; r < 2 && e == cudaSuccess; ++r) e = launch_step(b, sh, rs, 0);
     if (e == cudaSuccess) e = cudaEventRecord(e0, b->stream);
     for (int r = 0; r < 3 && e == cudaSuccess; ++r) e = launch_step(b, sh, rs, 0);
     if (e == cudaSuccess) e = cudaEventRecord(e1, b->stream);
@@ -482,33 +481,26 @@ int time_step(imex_batch* b, const BatchShape& sh, const RowShape& rs, float* ms
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (e != cudaSuccess) return bcuda(b, e, "batch autotune");
-    b->launches += 6 * ((b->n_cell > 0) + (b->n_row > 0));
+    b->launches += 4 * ((b->n_cell > 0) + (b->n_row > 0));
     *ms = t / 3;
     return IMEX_OK;
 }
 
-// Pick the launch shapes: the cell kernel's shape with every member in it,
-// then each row-kernel shape (members that suit it move to the row kernel,
-// the rest stay in the cell kernel), keeping the fastest step.  Shapes set
-// by imex_batch_set_launch / imex_batch_set_row_launch are kept.
+// Pick the launch shapes.  First the row kernel's: each shape, with and
+// without the float32 members, against the row kernel off, the members it
+// leaves in the cell kernel at the cell kernel's current (or default)
+// shape; then the cell kernel's shapes - only if the chosen split leaves it
+// members, and timed on that split.  Shapes pinned by imex_batch_set_launch
+// / imex_batch_set_row_launch are kept.  Each timing is one warm-up and
+// three steps of the whole batch, so the order matters for a large batch:
+// the row kernel usually takes every member, and the cell kernel's 15
+// shapes are then not timed at all.
 int tune_batch(imex_batch* b, bool tune_cells, bool tune_rows)
 {
     const RowShape off{-1, 0, 0, 1};
-    float best = 0.f;
-    if (tune_cells) {
-        BatchShape best_shape;
-        for (const BatchShape& sh : candidates()) {
-            float ms = 0.f;
-            int rc = time_step(b, sh, off, &ms);
-            if (rc) return rc;
-            if (!best_shape.threads || ms < best) {
-                best = ms;
-                best_shape = sh;
-            }
-        }
-        b->shape = best_shape;
-    }
+    if (!b->shape.threads) b->shape = BatchShape{256, 1, 8};
     if (tune_rows) {
+        float best = 0.f;
         int rc = time_step(b, b->shape, off, &best);
         if (rc) return rc;
         RowShape best_rs = off;
@@ -526,6 +518,25 @@ int tune_batch(imex_batch* b, bool tune_cells, bool tune_rows)
             }
         }
         b->rshape = best_rs;
+    }
+    if (tune_cells) {
+        std::vector<int> one(b->members.size(), 1);
+        int rc = upload_table(b, one, b->rshape);
+        if (rc) return rc;
+        if (b->n_cell > 0) {
+            float best = 0.f;
+            BatchShape best_shape;
+            for (const BatchShape& sh : candidates()) {
+                float ms = 0.f;
+                rc = time_step(b, sh, b->rshape, &ms);
+                if (rc) return rc;
+                if (!best_shape.threads || ms < best) {
+                    best = ms;
+                    best_shape = sh;
+                }
+            }
+            b->shape = best_shape;
+        }
     }
     return IMEX_OK;
 }
