@@ -36,6 +36,9 @@ _dp = ctypes.POINTER(ctypes.c_double)
 _h = ctypes.c_void_p
 
 
+IMEX_POLICY_ARRIVAL = 0
+IMEX_POLICY_LEAST_WORK = 1
+
 IMEX_PHASE_COLLISION = 0
 IMEX_PHASE_STREAM = 1
 IMEX_PHASE_MACRO = 2
@@ -144,6 +147,7 @@ SIGNATURES = {
     "imex_server_poll": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Result), ctypes.c_int,
                                         ctypes.POINTER(ctypes.c_int)]),
     "imex_server_get_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ServerStats)]),
+    "imex_server_set_policy": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "imex_server_now": (ctypes.c_double, [ctypes.c_void_p]),
     "imex_server_destroy": (None, [ctypes.c_void_p]),
 }

@@ -1,5 +1,7 @@
-// Row-staged fused step: persistent CTAs stream blocks of source rows
-// through a multi-stage shared-memory ring with asynchronous bulk copies.
+// Row-staged fused step of the float64 fixed-point engine (the reduced-
+// precision formats have their own, rows_lowp.cuh): persistent CTAs stream
+// blocks of source rows through a multi-stage shared-memory ring with
+// asynchronous bulk copies.
 //
 // The pull of cell (x, y, z) along direction a reads row (x - ex, y - ey) of
 // plane a, shifted by ez along z.  A work item is B consecutive destination
@@ -21,7 +23,7 @@
 // granularity), B dividing ny, S * 27 * B * nz * sizeof(T) bytes of shared
 // memory per CTA.
 //
-// Engine interface (one per storage/arithmetic pair):
+// Engine interface (EngFx, kernels_fx.cu):
 //   using T;                                    storage element type
 //   static constexpr int kMinBlocks;            resident CTAs of 256 threads
 //                                               the registers must allow

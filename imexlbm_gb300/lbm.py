@@ -345,6 +345,10 @@ class Server:
     def now(self) -> float:
         return float(self._L.imex_server_now(self._s))
 
+    def set_policy(self, policy: int) -> None:
+        """IMEX_POLICY_ARRIVAL (default) or IMEX_POLICY_LEAST_WORK admission."""
+        check(self._L.imex_server_set_policy(self._s, int(policy)))
+
     def close(self) -> None:
         if getattr(self, "_s", None):
             self._L.imex_server_destroy(self._s)

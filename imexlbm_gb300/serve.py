@@ -23,7 +23,7 @@ whole minute; the percentiles say so.
 
 Usage: python -m imexlbm_gb300.serve [--rate 50] [--duration 60]
           [--budget-gb 120] [--max-active 256] [--steps-per-tick 25]
-          [--spot 16] [--json out.json]
+          [--spot 16] [--policy arrival|least-work] [--json out.json]
        small trace: --edges 16,24,32 --steps-min 20 --steps-max 80
 """
 from __future__ import annotations
@@ -78,12 +78,13 @@ def run_alone(req, precision):
 
 
 def run(rate=50.0, duration=60.0, budget_gb=120.0, max_active=256, steps_per_tick=25, spot=16, seed=20261203,
-        edges=EDGES, steps_range=(200, 5000), drain_timeout=3600.0, log=print):
+        edges=EDGES, steps_range=(200, 5000), drain_timeout=3600.0, log=print, policy="arrival"):
     reqs = trace(rate, duration, seed, edges=edges, weights=WEIGHTS[:len(edges)] if len(edges) <= len(WEIGHTS)
                  else [1.0] * len(edges), steps_range=steps_range)
     results = {}
     peak_active = 0
     with Server(budget_gb * 1e9, max_active, steps_per_tick) as srv:
+        srv.set_policy({"arrival": _lib.IMEX_POLICY_ARRIVAL, "least-work": _lib.IMEX_POLICY_LEAST_WORK}[policy])
         t0 = time.perf_counter()
         ids = {}
         for i, r in enumerate(reqs):
@@ -124,7 +125,7 @@ def run(rate=50.0, duration=60.0, budget_gb=120.0, max_active=256, steps_per_tic
     out = {"requests": len(reqs), "completed": len(ok), "diverged": sum(r["status"] == _lib.IMEX_ERR_NONFINITE for r in done),
            "failed": len(done) - len(ran), "statuses": statuses, "unfinished": len(reqs) - len(done),
            "rate_per_s": rate, "duration_s": duration, "budget_gb": budget_gb, "max_active": max_active,
-           "steps_per_tick": steps_per_tick, "seed": seed, "submit_seconds": t_submitted,
+           "steps_per_tick": steps_per_tick, "policy": policy, "seed": seed, "submit_seconds": t_submitted,
            "ttr_p50_s": float(np.percentile(ttr, 50)), "ttr_p99_s": float(np.percentile(ttr, 99)),
            "ttr_max_s": float(ttr.max()), "aggregate_mlups": updates / span / 1e6 if ran else None,
            "busy_mlups": st["cell_updates"] / st["busy_seconds"] / 1e6 if st["busy_seconds"] else None,
@@ -180,10 +181,13 @@ def main(argv=None) -> int:
     ap.add_argument("--steps-min", type=int, default=200)
     ap.add_argument("--steps-max", type=int, default=5000)
     ap.add_argument("--drain-timeout", type=float, default=3600.0)
+    ap.add_argument("--policy", choices=["arrival", "least-work"], default="arrival",
+                    help="admission order: first come first served, or least work (cells x steps) first")
     ap.add_argument("--json", default=None)
     a = ap.parse_args(argv)
     r = run(a.rate, a.duration, a.budget_gb, a.max_active, a.steps_per_tick, a.spot, a.seed,
-            edges=tuple(int(x) for x in a.edges.split(",")), steps_range=(a.steps_min, a.steps_max), drain_timeout=a.drain_timeout)
+            edges=tuple(int(x) for x in a.edges.split(",")), steps_range=(a.steps_min, a.steps_max),
+            drain_timeout=a.drain_timeout, policy=a.policy)
     if a.json:
         with open(a.json, "w") as fp:
             json.dump(r, fp, indent=1)

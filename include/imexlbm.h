@@ -389,6 +389,15 @@ int imex_server_get_stats(imex_server *s, imex_server_stats *out);
 /* Seconds since the server started (the clock of the results' times). */
 double imex_server_now(const imex_server *s);
 
+/* Admission order: IMEX_POLICY_ARRIVAL (default, first come first served;
+ * the head waits for memory, no overtaking) or IMEX_POLICY_LEAST_WORK (the
+ * queued request with the fewest cells x steps first: a shorter median
+ * time-to-result under overload; large requests wait until the queue
+ * drains). */
+#define IMEX_POLICY_ARRIVAL 0
+#define IMEX_POLICY_LEAST_WORK 1
+int imex_server_set_policy(imex_server *s, int policy);
+
 /* Stop the server thread; requests still queued or running are dropped. */
 void imex_server_destroy(imex_server *s);
 

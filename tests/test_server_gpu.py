@@ -151,3 +151,17 @@ def _wait(srv, n, timeout=60):
         time.sleep(0.01)
     assert len(got) == n
     return got
+
+
+def test_least_work_policy_admits_small_requests_first(imex):
+    with imex.Server(budget_bytes=2e9, max_active=1, steps_per_tick=10) as srv:
+        srv.set_policy(imex.IMEX_POLICY_LEAST_WORK)
+        srv.submit(96, 96, 96, 0.004, 0.05, 3000, imex.IMEX_F32, tag=1)  # running while the others queue
+        time.sleep(0.02)
+        srv.submit(32, 32, 32, 0.004, 0.05, 200, imex.IMEX_F32, tag=2)   # more work
+        srv.submit(16, 16, 16, 0.004, 0.05, 20, imex.IMEX_F32, tag=3)    # least work, arrives last
+        got = _wait(srv, 3)
+    assert all(r["status"] == 0 for r in got.values())
+    assert got[3]["t_admit"] < got[2]["t_admit"]
+    with pytest.raises(imex.ImexError):
+        imex.Server(budget_bytes=1e8, max_active=1, steps_per_tick=5).set_policy(7)
