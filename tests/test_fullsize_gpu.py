@@ -1,0 +1,70 @@
+"""Properties at the benchmark's full size: the shipped deck's 256^3 lattice.
+
+The oracle is too slow at this size for a test (about 90 MLUPS on 16 host
+cores), so these checks use what holds whatever the size:
+- the two float64 engines - exact fixed point on the integer pipes and
+  native float64 FMA arithmetic, written independently - agree on every f
+  to 1e-12 relative after 100 steps;
+- mass is invariant to 1e-12 and momentum stays zero to the regression
+  tolerance (tests/regression.sh of the reference: 1e-12, 1e-10);
+- the Taylor-Green kinetic energy decays at every report step;
+- the reduced-precision formats stay within their stated kinetic-energy and
+  mass tolerances of the float64 run.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+N = 256
+STEPS = 100
+
+
+def deck(imex):
+    return imex.System(text=f"1.0 0.1 1600\n0.05 {STEPS} 20\n{N} {N} {N}\n")
+
+
+def test_engines_agree_and_invariants_hold(imex):
+    torch = pytest.importorskip("torch")
+    d = deck(imex)
+    n = 27 * N ** 3
+    fields = {}
+    for eng in (imex.IMEX_ENGINE_FIXED, imex.IMEX_ENGINE_NATIVE):
+        with imex.LBM(N, N, N, d.tau, d.rho0, d.u0, engine=eng) as lat:
+            lat.Initialize()
+            m0 = lat.Conserved()[0]
+            kes = []
+            for _ in range(STEPS // 20):
+                lat.step(20)
+                mass, px, py, pz, ke = lat.Conserved()
+                assert abs(mass - m0) <= 1e-12 * m0
+                assert max(abs(px), abs(py), abs(pz)) <= 1e-10 * m0
+                kes.append(ke)
+            assert all(b < a for a, b in zip(kes, kes[1:])), kes
+            buf = torch.empty(n, dtype=torch.float64, device="cuda")
+            torch.cuda.synchronize()
+            lat.get_f_device(buf.data_ptr(), n)
+            fields[eng] = buf
+            if eng == imex.IMEX_ENGINE_FIXED:
+                assert lat.fallback_cells() == 0
+    a, b = fields[imex.IMEX_ENGINE_FIXED], fields[imex.IMEX_ENGINE_NATIVE]
+    rel = ((a - b).abs() / b.abs()).max().item()
+    assert rel <= 1e-12, rel
+
+
+@pytest.mark.parametrize("name,ke_tol,mass_tol", [("f32", 2e-5, 1e-8), ("f16dev", 2e-4, 1e-6)])
+def test_reduced_precision_against_float64(imex, name, ke_tol, mass_tol):
+    d = deck(imex)
+    prec = {"f32": imex.IMEX_F32, "f16dev": imex.IMEX_F16DEV}[name]
+    with imex.LBM(N, N, N, d.tau, d.rho0, d.u0) as ref, \
+            imex.LBM(N, N, N, d.tau, d.rho0, d.u0, precision=prec) as lat:
+        ref.Initialize()
+        lat.Initialize()
+        m0 = lat.Conserved()[0]
+        ref.step(STEPS)
+        lat.step(STEPS)
+        want, got = ref.Conserved(), lat.Conserved()
+        du, umax = lat.velocity_max_diff(ref)
+    assert abs(got[4] - want[4]) <= ke_tol * want[4]
+    assert abs(got[0] - m0) <= mass_tol * m0
+    assert du <= 5e-3 * d.u0 and 0.5 * d.u0 < umax < 1.5 * d.u0
