@@ -104,8 +104,7 @@ __device__ __forceinline__ void batch_cell(const BatchEntry& e, unsigned long lo
     lowp::collide_dev_f32<P>(h, cp);
     if constexpr (P == IMEX_F16DEV) {
         auto at = [&](int a) -> T& { return dst[(size_t)a * e.plane + local]; };
-        if (e.sr) lowp::store_f16_cell_sr(h, local, e.seed + (uint32_t)s, at);
-        else lowp::store_f16_cell(h, at);
+        lowp::store_f16_cell(h, e.sr, local, e.seed + (uint32_t)s, at);
     } else {
 #pragma unroll
         for (int a = 0; a < kQ; ++a) dst[(size_t)a * e.plane + local] = S::store(h[a], a);

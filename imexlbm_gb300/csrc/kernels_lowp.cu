@@ -47,12 +47,11 @@ __global__ void __launch_bounds__(kStepBlock) k_step_lowp(const typename Storage
     collide_dev_f32<P>(h, cp);
     if constexpr (P == IMEX_F16DEV) {
         auto at = [&](int a) -> __half& { return dst[(size_t)a * g.plane + cell]; };
-        if (cp.sr) lowp::store_f16_cell_sr(h, cell, cp.seed, at);
-        else lowp::store_f16_cell(h, at);
-        return;
-    }
+        lowp::store_f16_cell(h, cp.sr, cell, cp.seed, at);
+    } else {
 #pragma unroll
-    for (int a = 0; a < kQ; ++a) dst[(size_t)a * g.plane + cell] = S::store(h[a], a);
+        for (int a = 0; a < kQ; ++a) dst[(size_t)a * g.plane + cell] = S::store(h[a], a);
+    }
 }
 
 // Taylor-Green initial state (float64 equilibrium, src/lbm.cpp:78-108),

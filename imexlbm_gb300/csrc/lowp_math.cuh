@@ -56,25 +56,37 @@ __device__ __forceinline__ uint32_t sr_hash(unsigned long long idx, uint32_t see
 // Random bits of the stochastic rounding, shared by every kernel so that a
 // lattice's result does not depend on which kernel stepped it: cells 2p and
 // 2p + 1 of a lattice (flat index, z fastest) share the 32-bit word
-// sr_word(hash(p, step), a) = hash + a * phi for direction a (phi = 2^32 /
+// sr_word(hash(p, step), ., a) = hash + a * phi for direction a (phi = 2^32 /
 // golden ratio, a Weyl sequence: each word uniform because the hash is;
 // across a pair's directions the draws are stratified rather than
 // independent).  Cell 2p takes bits 0..12 and cell 2p + 1 bits 16..28 -
 // the operand layout of cvt.rs.f16x2.f32 with cell 2p in the low half.
-__device__ __forceinline__ uint32_t sr_word(uint32_t pair_hash, int a) { return pair_hash + (uint32_t)a * 0x9E3779B9u; }
+//
+// The eight corner populations (directions kFirstCorner..26) absorb the
+// other populations' rounding errors before they are rounded themselves
+// (round_f16_conserving).  A corner's draw must then be independent of the
+// others' draws: the low bits of hash + a * phi are a function of the low
+// bits of the hash alone, and a corner draw tied to the draws that set its
+// correction would round it up more often than its value asks (a kinetic-
+// energy drift of ~4e-6 per 1000 steps at 512^3).  The corners therefore
+// draw from a second word of the pair, sr_corner_hash(hash), a full mix of
+// all 32 bits.
+constexpr int kFirstCorner = 2 * 10 - 1;  // pairs 10..13 are the corners (d3q27.cuh)
 
-// Store 27 float16 deviations of one cell, converting two at a time
-// (values already on the float16 grid convert exactly).
-template <class Dst>
-__device__ __forceinline__ void store_f16_cell(const float (&y)[kQ], Dst&& at)
+__device__ __forceinline__ uint32_t sr_corner_hash(uint32_t pair_hash)
 {
-#pragma unroll
-    for (int a = 0; a + 1 < kQ; a += 2) {
-        const __half2 v = __floats2half2_rn(y[a], y[a + 1]);
-        at(a) = __low2half(v);
-        at(a + 1) = __high2half(v);
-    }
-    at(kQ - 1) = __float2half_rn(y[kQ - 1]);
+    uint32_t x = pair_hash ^ 0x5BD1E995u;
+    x ^= x >> 16;
+    x *= 0x7FEB352Du;
+    x ^= x >> 15;
+    x *= 0x846CA68Bu;
+    x ^= x >> 16;
+    return x;
+}
+
+__device__ __forceinline__ uint32_t sr_word(uint32_t pair_hash, uint32_t corner_hash, int a)
+{
+    return (a >= kFirstCorner ? corner_hash : pair_hash) + (uint32_t)a * 0x9E3779B9u;
 }
 
 // Stochastic rounding of a float32 pair to float16 in one instruction
@@ -92,22 +104,6 @@ __device__ __forceinline__ uint32_t cvt_rs_f16x2(float hi, float lo, uint32_t rb
     uint32_t d;
     asm("cvt.rs.f16x2.f32 %0, %1, %2, %3;" : "=r"(d) : "f"(hi), "f"(lo), "r"(rbits));
     return d;
-}
-
-// Store 27 float16 deviations of one cell with stochastic rounding: the
-// cell's half of its pair's random words (see sr_word).
-template <class Dst>
-__device__ __forceinline__ void store_f16_cell_sr(const float (&y)[kQ], unsigned long long cell, uint32_t seed,
-                                                  Dst&& at)
-{
-    const uint32_t ph = sr_hash(cell >> 1, seed);
-    const bool odd = cell & 1;
-#pragma unroll
-    for (int a = 0; a < kQ; ++a) {
-        const uint32_t w = sr_word(ph, a);
-        const uint32_t d = odd ? cvt_rs_f16x2(y[a], 0.0f, w) >> 16 : cvt_rs_f16x2(0.0f, y[a], w) & 0xffffu;
-        at(a) = __ushort_as_half((unsigned short)d);
-    }
 }
 
 // kScale: the collision works on kScale * (f - w).  float32 storage keeps f
@@ -244,6 +240,109 @@ template <int P>
 __device__ __forceinline__ void collide_dev_f32(float (&h)[kQ], const CollideF32& cp)
 {
     collide_dev<P, F1>(h, cp);
+}
+
+// float(r) - v for a float16 r and a float32 v in one instruction (the
+// mixed-precision sub.f32.f16 of the sm_100 family: r widens exactly, then
+// one rounding, as in __fsub_rn(__half2float(r), v)).
+__device__ __forceinline__ float sub_f16_f32(__half r, float v)
+{
+    float d;
+    asm("sub.rn.f32.f16 %0, %1, %2;" : "=f"(d) : "h"(__half_as_ushort(r)), "f"(v));
+    return d;
+}
+
+// Rounding of one cell's (A = F1) or two cells' (A = F2) 27 float32
+// deviations to float16 that keeps each cell's momentum.
+//
+// A float16 step of an axis or face-diagonal population is 4 to 16 times
+// that of a corner population (the deviations scale with the weights 2/27,
+// 1/54, 1/216).  Rounding every value on its own leaves a momentum error of
+// the order of an axis population's step in every cell and every step; that
+// noise drives the flow, and on coarse lattices over a few thousand steps
+// it moved the kinetic energy by up to 2.4e-4 from the float64 result.
+// Here the 19 rest, axis and face-diagonal populations are rounded first
+// and the momentum of their rounding errors is summed, p = sum e_a (r_a -
+// y_a).  The eight corner populations s = (+-1, +-1, +-1) absorb it before
+// they are rounded: each moves by -s.p / 8, and since the corners' s sum to
+// 0 and their s s^T to 8 I, the moves take p out of the momentum exactly and
+// leave the mass alone.  What remains is the corners' own rounding, 4 to 16
+// times smaller.  The moves are a few float16 steps of a corner population;
+// under stochastic rounding the errors they undo have zero mean and the
+// corners draw independent random bits (sr_corner_hash), so the corners
+// stay unbiased.  (Taking the mass error into the corners as well, by
+// -(m + s.p) / 8, cost 3% of the step and did not lower the kinetic-energy
+// error further.)
+//
+// `rnd(a, v)` rounds v (for direction a) to float16, stores it, and returns
+// the rounding error r - v (exact: r and v are within a float16 step of
+// each other).  The sums use A's operations in a fixed order, so one-cell
+// and two-cell kernels store the same bits.
+template <class A, class Rnd>
+__device__ __forceinline__ void round_f16_conserving(const typename A::V (&y)[kQ], Rnd&& rnd)
+{
+    using V = typename A::V;
+    // D_k = r_a - y_a - (r_b - y_b) for the 9 non-corner pairs (a, b) =
+    // (2k - 1, 2k): the pair's momentum error along e_a.  The rest
+    // population carries no momentum.
+    V D[10];
+    rnd(0, y[0]);
+#pragma unroll
+    for (int k = 1; k < 10; ++k) {
+        const V da = rnd(2 * k - 1, y[2 * k - 1]);
+        const V db = rnd(2 * k, y[2 * k]);
+        D[k] = A::sub(da, db);
+    }
+    // p[dim] = sum over the five pairs moving along dim of e_dim D_k, the
+    // axis pair (e_dim = +1) first
+    V p[3];
+#pragma unroll
+    for (int dim = 0; dim < 3; ++dim) {
+        V acc = D[dim + 1];
+#pragma unroll
+        for (int k = 4; k < 10; ++k) {
+            const int e = ex(2 * k - 1, dim);
+            if (e == 1) acc = A::add(acc, D[k]);
+            else if (e == -1) acc = A::sub(acc, D[k]);
+        }
+        p[dim] = acc;
+    }
+    const V neg8 = A::splat(-0.125f);
+#pragma unroll
+    for (int a = kFirstCorner; a < kQ; a += 2) {
+        // s.p for the pair's first member s; the opposite member has -s.p
+        const V sx = ex(a, 0) == 1 ? p[0] : A::sub(A::splat(0.f), p[0]);
+        const V sxy = ex(a, 1) == 1 ? A::add(sx, p[1]) : A::sub(sx, p[1]);
+        const V sp = ex(a, 2) == 1 ? A::add(sxy, p[2]) : A::sub(sxy, p[2]);
+        rnd(a, A::fma(neg8, sp, y[a]));
+        rnd(a + 1, A::fma(neg8, A::sub(A::splat(0.f), sp), y[a + 1]));
+    }
+}
+
+// Store the 27 float16 deviations of one cell (flat index `cell`), rounded
+// to nearest or stochastically (the cell's half of its pair's random words,
+// see sr_word), through round_f16_conserving.
+template <class Dst>
+__device__ __forceinline__ void store_f16_cell(const float (&y)[kQ], bool sr, unsigned long long cell, uint32_t seed,
+                                               Dst&& at)
+{
+    if (sr) {
+        const uint32_t ph = sr_hash(cell >> 1, seed), pc = sr_corner_hash(ph);
+        const bool odd = cell & 1;
+        round_f16_conserving<F1>(y, [&](int a, float v) -> float {
+            const uint32_t w = sr_word(ph, pc, a);
+            const uint32_t d = odd ? cvt_rs_f16x2(v, 0.0f, w) >> 16 : cvt_rs_f16x2(0.0f, v, w) & 0xffffu;
+            const __half r = __ushort_as_half((unsigned short)d);
+            at(a) = r;
+            return sub_f16_f32(r, v);
+        });
+    } else {
+        round_f16_conserving<F1>(y, [&](int a, float v) -> float {
+            const __half r = __float2half_rn(v);
+            at(a) = r;
+            return sub_f16_f32(r, v);
+        });
+    }
 }
 
 }  // namespace lowp

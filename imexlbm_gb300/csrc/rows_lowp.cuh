@@ -150,17 +150,23 @@ __device__ __forceinline__ void compute_item(const unsigned char* __restrict__ i
         lowp::collide_dev<P, Ar>(h, cp);
         T* o = reinterpret_cast<T*>(it.dst) + row0 + (size_t)b * nz + z;
         if constexpr (P == IMEX_F16DEV) {
-            const uint32_t ph = cp.sr ? lowp::sr_hash((row0 + (unsigned long long)b * nz + z) >> 1, cp.seed) : 0u;
-#pragma unroll
-            for (int a = 0; a < kQ; ++a) {
-                uint32_t w;
-                if (cp.sr) {
-                    w = lowp::cvt_rs_f16x2(h[a].y, h[a].x, lowp::sr_word(ph, a));
-                } else {
-                    const __half2 v = __floats2half2_rn(h[a].x, h[a].y);
-                    w = *reinterpret_cast<const uint32_t*>(&v);
-                }
-                *reinterpret_cast<uint32_t*>(o + (size_t)a * it.plane) = w;
+            // one rounding loop per mode (a branch per direction costs
+            // issue slots in this instruction-heavy loop)
+            if (cp.sr) {
+                const uint32_t ph = lowp::sr_hash((row0 + (unsigned long long)b * nz + z) >> 1, cp.seed);
+                const uint32_t pc = lowp::sr_corner_hash(ph);
+                lowp::round_f16_conserving<Ar>(h, [&](int a, float2 v) -> float2 {
+                    const uint32_t w = lowp::cvt_rs_f16x2(v.y, v.x, lowp::sr_word(ph, pc, a));
+                    const __half2 r = *reinterpret_cast<const __half2*>(&w);
+                    *reinterpret_cast<__half2*>(o + (size_t)a * it.plane) = r;
+                    return make_float2(lowp::sub_f16_f32(__low2half(r), v.x), lowp::sub_f16_f32(__high2half(r), v.y));
+                });
+            } else {
+                lowp::round_f16_conserving<Ar>(h, [&](int a, float2 v) -> float2 {
+                    const __half2 r = __floats2half2_rn(v.x, v.y);
+                    *reinterpret_cast<__half2*>(o + (size_t)a * it.plane) = r;
+                    return make_float2(lowp::sub_f16_f32(__low2half(r), v.x), lowp::sub_f16_f32(__high2half(r), v.y));
+                });
             }
         } else {
 #pragma unroll

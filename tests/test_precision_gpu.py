@@ -107,8 +107,16 @@ def test_call_sequences_and_macroscopic(imex, oracle, name):
                 f = oracle.stream(f)
         got = lat.get_f()
         p, u, v, w = lat.ComputeMacroscopic()
-    tol = 1e-6 if prec == imex.IMEX_F32 else 2e-4
-    assert np.max(np.abs(got - f) / weights(oracle)) <= tol
+    wts = weights(oracle)
+    if prec == imex.IMEX_F32:
+        assert np.max(np.abs(got - f) / wts) <= 1e-6
+    else:
+        # every population within 2e-4 of its weight; the corner populations,
+        # which take up the other populations' momentum rounding errors,
+        # within 2e-4 of the axis weight
+        corner = np.abs(oracle.velocities()).sum(1) == 3
+        scale = np.where(corner[:, None, None, None], wts[1], wts)
+        assert np.max(np.abs(got - f) / scale) <= 2e-4
     for a, b in zip((u, v, w), oracle.macroscopic(got)[1:]):
         assert np.max(np.abs(a - b)) <= 1e-12
 
@@ -157,6 +165,45 @@ def test_stochastic_rounding_keeps_ke_on_the_deck(imex, oracle):
     w = oracle.conserved(f)
     assert abs(c[4] - w[4]) <= 1e-4 * w[4]
     assert abs(c[0] - m0) <= 1e-6 * m0
+
+
+def f16_step(x):
+    """Spacing of float16 numbers at |x| (normal range)."""
+    return 2.0 ** (np.floor(np.log2(np.maximum(np.abs(x), 2.0 ** -14))) - 10)
+
+
+@pytest.mark.parametrize("rounding", ["nearest", "stochastic"])
+def test_float16_rounding_keeps_cell_momentum(imex, oracle, rounding):
+    """The float16 rounding moves the momentum of the rounding errors of the
+    rest, axis and face-diagonal populations into the eight corner
+    populations: after one collision each cell's momentum equals the float64
+    collision's to the corners' own rounding, far below one float16 step of
+    an axis population (what rounding every value on its own leaves)."""
+    shape = (8, 10, 12)
+    tau = 0.01
+    rng = np.random.default_rng(5)
+    w = weights(oracle)
+    f = oracle.init(*shape, 1.0, 0.08)
+    f = stored(oracle, imex.IMEX_F16DEV, imex, f + 1e-3 * w * rng.standard_normal(f.shape))
+    with imex.LBM(*shape, tau, 1.0, 0.08, precision=imex.IMEX_F16DEV) as lat:
+        lat.set_rounding(imex.IMEX_ROUND_NEAREST if rounding == "nearest" else imex.IMEX_ROUND_STOCHASTIC)
+        lat.set_f(f)
+        lat.Collision()
+        got = lat.get_f()
+    want = f.copy()
+    oracle.collide(want, tau)
+    e = oracle.velocities().astype(np.float64)
+    du = np.tensordot(e.T, got - want, axes=1)
+    H = (want - w) * 4096.0
+    corner = np.abs(e).sum(1) == 3
+    axis = np.abs(e).sum(1) == 1
+    corner_step = f16_step(np.abs(H[corner]).max(0)) / 4096.0
+    axis_step = f16_step(np.abs(H[axis]).max(0)) / 4096.0
+    # each corner rounds once (one step at most); the float32 collision's own
+    # error is far below
+    assert np.all(np.abs(du) <= (8 * corner_step + 1e-9)[None])
+    rms = np.sqrt(np.mean(du ** 2))
+    assert rms <= 0.2 * np.sqrt(np.mean(axis_step ** 2)), rms
 
 
 def test_stochastic_rounding_needs_float16(imex):
