@@ -177,8 +177,14 @@ struct F2 {
 // carry 1 / kScale, folded into their constants.  kScale is a power of two,
 // so every intermediate is exactly kScale^k times the unscaled one and the
 // result is exactly kScale times the unscaled collision's: both storage
-// formats run the same float32 arithmetic.  2 heq - h is formed as
-// (heq + heq) - h: heq + heq is exact, so it rounds like fma(2, heq, -h).
+// formats run the same float32 arithmetic.
+//
+// Per population, with t = h - heq: h <- heq - t + eps t, formed as
+// fma(eps, t, heq - t) - three operations, each rounding below the
+// population's own size (t, the non-equilibrium part, is small).  The
+// equilibrium of an opposite pair is A +- B with A = w (4.5 (e.u)^2 / kScale
+// + base) = (w 4.5 / kScale) (e.u)^2 + w base and B = b (e.u), each side one
+// fused multiply-add: fma(+-b, e.u, A).
 template <int P, class A>
 __device__ __forceinline__ void collide_dev(typename A::V (&h)[kQ], const CollideF32& cp)
 {
@@ -209,9 +215,12 @@ __device__ __forceinline__ void collide_dev(typename A::V (&h)[kQ], const Collid
     const V udu = A::fma(u[2], u[2], A::fma(u[1], u[1], A::mul(u[0], u[0])));
     const V base = A::fma(A::splat(c15), udu, sig);
     const V eps = A::splat(cp.eps);
+    // w base for the four weight classes (rest, axis, face diagonal, corner)
+    const V wb[4] = {A::mul(A::splat(cp.w[0]), base), A::mul(A::splat(cp.w[1]), base),
+                     A::mul(A::splat(cp.w[2]), base), A::mul(A::splat(cp.w[3]), base)};
     {
-        const V heq = A::mul(A::splat(cp.w[0]), base);
-        h[0] = A::fma(eps, A::sub(h[0], heq), A::sub(A::add(heq, heq), h[0]));
+        const V t = A::sub(h[0], wb[0]);
+        h[0] = A::fma(eps, t, A::sub(wb[0], t));
     }
 #pragma unroll
     for (int k = 1; k <= kPairs; ++k) {
@@ -228,11 +237,11 @@ __device__ __forceinline__ void collide_dev(typename A::V (&h)[kQ], const Collid
                 first = false;
             }
         }
-        const V Aq = A::mul(A::splat(cp.w[cls]), A::fma(A::mul(A::splat(c45), edu), edu, base));
-        const V Bq = A::mul(A::splat(cp.w3[cls]), edu);
-        const V ep = A::add(Aq, Bq), em = A::sub(Aq, Bq);
-        h[a] = A::fma(eps, A::sub(h[a], ep), A::sub(A::add(ep, ep), h[a]));
-        h[a + 1] = A::fma(eps, A::sub(h[a + 1], em), A::sub(A::add(em, em), h[a + 1]));
+        const V Aq = A::fma(A::mul(A::splat(cp.w[cls] * c45), edu), edu, wb[cls]);
+        const V ep = A::fma(A::splat(cp.w3[cls]), edu, Aq), em = A::fma(A::splat(-cp.w3[cls]), edu, Aq);
+        const V tp = A::sub(h[a], ep), tm = A::sub(h[a + 1], em);
+        h[a] = A::fma(eps, tp, A::sub(ep, tp));
+        h[a + 1] = A::fma(eps, tm, A::sub(em, tm));
     }
 }
 

@@ -237,8 +237,10 @@ int imex_set_engine(imex_lattice *h, int engine);
  * omega close to 2 (high Reynolds number) the non-equilibrium part of each
  * population is far below half a float16 step of f - w, so rounding to
  * nearest erases it deterministically and biases the viscous decay (512^3,
- * Re 1600: kinetic energy off by 9e-8 per step); stochastic rounding keeps
- * it in expectation (4e-9 after 1000 steps) at some throughput.  The random
+ * Re 1600: kinetic energy off by 9e-9 per step); stochastic rounding keeps
+ * it in expectation (1.3e-8 after 1000 steps).  Both modes keep each cell's
+ * momentum: the momentum of the other populations' rounding errors is moved
+ * into the eight corner populations before they are rounded.  The random
  * bits come from a hash of (cell, step), so runs are reproducible and
  * identical across kernels and batches. */
 int imex_set_rounding(imex_lattice *h, int mode);
