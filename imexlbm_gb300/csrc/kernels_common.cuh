@@ -21,6 +21,17 @@ struct Geom {
 // cells of one (x, y) row; grid = (ceil(nz / kStepBlock), ny, nx).
 constexpr int kStepBlock = 128;
 
+// SM count of the calling thread's current device, for persistent grids.
+// Queried per call: the runtime answers from its own cache, and a process
+// that drives several devices gets each one's count.
+inline int current_sm_count()
+{
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 1;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1) return 1;
+    return sms;
+}
+
 // Source indices of the pull for cell (i, j, k): the value streaming into
 // the cell along direction a comes from (i - ex, j - ey, k - ez), wrapped
 // periodically.  This is the one-rank image of the reference's ghost layer

@@ -223,7 +223,7 @@ cudaError_t launch_maxdiff3(const double* a, const double* b, size_t n, unsigned
 {
     cudaError_t e = cudaMemsetAsync(out, 0, 2 * sizeof(unsigned long long), s);
     if (e != cudaSuccess) return e;
-    k_maxdiff3<<<152 * 8, 256, 0, s>>>(a, b, n, out);
+    k_maxdiff3<<<current_sm_count() * 8, 256, 0, s>>>(a, b, n, out);
     return cudaGetLastError();
 }
 

@@ -267,12 +267,7 @@ cudaError_t launch_rows_lowp_d(int prec, const void* src, void* dst, const Geom&
 cudaError_t launch_rows_lowp(int prec, const void* src, void* dst, const Geom& g, const CollideF32& cp,
                              const RowConfig& rc, unsigned* err, cudaStream_t s)
 {
-    static int sms = 0;
-    if (!sms) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    }
+    const int sms = current_sm_count();
     const size_t es = prec == IMEX_F32 ? 4 : 2;
     if (rc.rows < 1 || (size_t)rc.rows * g.nz * es > (size_t)rc.dir_bytes || rc.stages < 2)
         return cudaErrorInvalidValue;
@@ -296,7 +291,7 @@ size_t rows_lowp_stage_bytes(int prec, int nz) { return (size_t)kQ * nz * (prec 
 
 cudaError_t launch_from_f64(int prec, const double* f, void* out, const Geom& g, cudaStream_t s)
 {
-    const int blocks = 152 * 8;
+    const int blocks = current_sm_count() * 8;
     if (prec == IMEX_F32)
         k_from_f64<IMEX_F32><<<blocks, 256, 0, s>>>(f, static_cast<float*>(out), g.plane);
     else

@@ -163,12 +163,7 @@ cudaError_t launch_rows(const typename E::T* src, typename E::T* dst, const Geom
                         unsigned* err, cudaStream_t s)
 {
     using T = typename E::T;
-    static int sms = 0;
-    if (!sms) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    }
+    const int sms = current_sm_count();
     const size_t smem = rows_smem_bytes<T>(g.nz, rc.stages, rc.rows);
     cudaError_t e = cudaFuncSetAttribute(k_rows<E>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;

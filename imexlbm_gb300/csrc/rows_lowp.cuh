@@ -19,9 +19,11 @@
 // Items of 2 KB per direction (B = 4 rows of 256 float16 values) measured
 // 296 us per 256^3 float16 step (57 GLUPS, 91% of the copy bandwidth);
 // 1 KB items 369 us; staging the outputs in shared memory for bulk stores
-// instead of storing them directly, 403 us.  Stochastic rounding packs the
-// pair with cvt.rs.f16x2.f32 and the pair's random word (sr_word), the
-// same bits the one-cell kernels use.
+// instead of storing them directly, 403 us; 4 KB items (B = 8), 283 us
+// (59.3 GLUPS).  Float16 results go through round_f16_conserving (each
+// cell's momentum kept); stochastic rounding packs the pair with
+// cvt.rs.f16x2.f32 and the pair's random words (sr_word), the same bits the
+// one-cell kernels use.
 //
 // Requirements: nz * element size a multiple of 16 bytes (so nz is even and
 // every run is 16-byte aligned), B * nz * element size <= kDirBytes.  B
