@@ -299,12 +299,14 @@ def run_ours(a):
     value = job_mlups(cells, a.steps, world, t_max * 1e-3)
     cons = lat.Conserved()
 
-    # roofline of the fused step kernel: every timed launch is that kernel
+    # roofline of the fused step kernel: every timed launch is that kernel (the
+    # fixed-point engine's run of steps: k_step_fxs, whose first and last
+    # launches read / write float64)
     hbm, peak_kind = load_peaks()
     launch_ms = ms / max(1, gpu_launches)
     bpc = BYTES_PER_CELL[a.precision]
     achieved = bpc * cells / (launch_ms * 1e-3) / 1e9
-    kname = {"fixed": "step_fx", "native": "step_f64", "float32": "step_lowp_" + a.precision}[eng_name]
+    kname = {"fixed": "step_fxs", "native": "step_f64", "float32": "step_lowp_" + a.precision}[eng_name]
     tr = load_traffic(kname)
     roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
             "frac": round(achieved / hbm, 4), "peak_kind": peak_kind,

@@ -99,16 +99,28 @@ IMEX_HD double double_of(uint32_t hi, uint32_t lo)
 }
 
 // ---- conversions ---------------------------------------------------------
-// float64 -> X for values whose shift s is in [0, smax]; clears ok
-// otherwise.  The sign bit is part of (hi >> 20), so negatives fail.
-IMEX_HD uint64_t to_fixed(double v, uint32_t smax, bool& ok)
+// float64 (bit pattern b) -> X for values whose shift s is in [0, smax];
+// clears ok otherwise.  The sign bit is part of (hi >> 20), so negatives
+// fail.
+IMEX_HD uint64_t to_fixed_bits(uint64_t b, uint32_t smax, bool& ok)
 {
-    const uint64_t b = bits_of(v);
     const uint32_t lo = (uint32_t)b, hi = (uint32_t)(b >> 32);
     const uint32_t s = (hi >> 20) - kInShift;
     ok = ok && (s <= smax);
     const uint32_t mh = (hi & 0x000FFFFFu) | 0x00100000u;
     return ((uint64_t)fshl(lo, mh, s) << 32) | fshl(0u, lo, s);
+}
+
+IMEX_HD uint64_t to_fixed(double v, uint32_t smax, bool& ok) { return to_fixed_bits(bits_of(v), smax, ok); }
+
+// A value already held as X (float64 precision, see round_fixed): the range
+// check to_fixed makes on the float64 it stands for, 2^52 <= X < 2^(53 +
+// smax), i.e. f in [2^-9, 2^(smax - 8)).
+IMEX_HD uint64_t check_fixed(uint64_t x, uint32_t smax, bool& ok)
+{
+    const uint32_t hi = (uint32_t)(x >> 32);
+    ok = ok && (hi - 0x00100000u) < ((0x00200000u << smax) - 0x00100000u);
+    return x;
 }
 
 // X -> float64 rounded to nearest (ties away from zero) for
@@ -122,6 +134,21 @@ IMEX_HD double from_fixed(uint64_t y, bool& ok)
     const uint64_t t = y + half;
     const uint32_t tl = (uint32_t)t, th = (uint32_t)(t >> 32);
     return double_of(fshr(th, 0u, r) + (r << 20) + kOutExp, fshr(tl, th, r));
+}
+
+// X -> X rounded to the float64 grid, to nearest with ties away from zero
+// (the value from_fixed would return, still in fixed point: the low r bits,
+// those below the 53-bit mantissa, cleared after adding half of their
+// weight); clears ok outside 2^52 <= X < 2^63.  to_fixed(from_fixed(y)) ==
+// round_fixed(y) for every y whose result is in range.
+IMEX_HD uint64_t round_fixed(uint64_t y, bool& ok)
+{
+    const uint32_t yh = (uint32_t)(y >> 32);
+    const uint32_t r = 11u - clz32(yh);
+    ok = ok && (r <= 10u);
+    const uint32_t unit = fshl(0u, 1u, r);  // 2^r (r <= 10)
+    const uint64_t t = y + (unit >> 1);
+    return t & ~(uint64_t)(unit - 1u);
 }
 
 // ---- products ------------------------------------------------------------
@@ -170,15 +197,19 @@ IMEX_HD constexpr int wclass(int a)
 }
 
 // ---- one cell ------------------------------------------------------------
-// BGK collision of the 27 values in f (reference direction order) into
-// out.  OM_GE1: omega >= 1, so (1 - omega) f is subtracted.  Clears ok when
-// the cell leaves the exact range (out is then meaningless).
-template <bool OM_GE1>
-IMEX_HD void collide_cell(const double (&f)[kQ], double (&out)[kQ], const FxConst& c, bool& ok)
+// BGK collision of the 27 values in `in` (reference direction order) into
+// out.  OM_GE1: omega >= 1, so (1 - omega) f is subtracted.  IN_FX / OUT_FX:
+// the values are held as X on the float64 grid (round_fixed), otherwise as
+// float64 bit patterns; both hold the same numbers, so the four encodings
+// give the same results.  Clears ok when the cell leaves the exact range
+// (out is then meaningless).
+template <bool OM_GE1, bool IN_FX, bool OUT_FX>
+IMEX_HD void collide_cell_io(const uint64_t (&in)[kQ], uint64_t (&out)[kQ], const FxConst& c, bool& ok)
 {
     uint64_t X[kQ];
 #pragma unroll
-    for (int a = 0; a < kQ; ++a) X[a] = to_fixed(f[a], a == 0 ? 8u : 5u, ok);
+    for (int a = 0; a < kQ; ++a)
+        X[a] = IN_FX ? check_fixed(in[a], a == 0 ? 8u : 5u, ok) : to_fixed_bits(in[a], a == 0 ? 8u : 5u, ok);
 
     // Exact moments.  G[x][y] sums the z-members of each (ex, ey) column;
     // every unsigned sum stays below 2^64 in the exact range.
@@ -237,7 +268,18 @@ IMEX_HD void collide_cell(const double (&f)[kQ], double (&out)[kQ], const FxCons
         o[a + 1] = OM_GE1 ? T - R - M2 : T - R + M2;
     }
 #pragma unroll
-    for (int a = 0; a < kQ; ++a) out[a] = from_fixed(o[a], ok);
+    for (int a = 0; a < kQ; ++a) out[a] = OUT_FX ? round_fixed(o[a], ok) : bits_of(from_fixed(o[a], ok));
+}
+
+template <bool OM_GE1>
+IMEX_HD void collide_cell(const double (&f)[kQ], double (&out)[kQ], const FxConst& c, bool& ok)
+{
+    uint64_t in[kQ], o[kQ];
+#pragma unroll
+    for (int a = 0; a < kQ; ++a) in[a] = bits_of(f[a]);
+    collide_cell_io<OM_GE1, false, false>(in, o, c, ok);
+#pragma unroll
+    for (int a = 0; a < kQ; ++a) out[a] = double_of((uint32_t)(o[a] >> 32), (uint32_t)o[a]);
 }
 
 }  // namespace fx

@@ -10,6 +10,16 @@ namespace imex {
 
 cudaError_t launch_step_fx(int mode, const double* src, double* dst, const Geom& g, const FxParams& fx,
                            const CollideF64& cp, unsigned long long* fallback, cudaStream_t s);
+// Launch j (1-based) of a run of n >= 2 fused steps whose state is held as
+// X on the float64 grid between launches (launch 1 reads float64, launch n
+// writes float64).  *fail must be above n before launch 1; it ends as the
+// first step whose cell left the exact range (the run's later launches do
+// nothing, and the state after step *fail - 1 is in that step's source
+// buffer, as X unless *fail is 1).
+cudaError_t launch_step_fx_run(const double* src, double* dst, const Geom& g, const FxParams& fx, int j, int n,
+                               int* fail, cudaStream_t s);
+// X on the float64 grid -> float64, in place, n values.
+cudaError_t launch_fx_to_f64(double* buf, size_t n, cudaStream_t s);
 struct RowConfig;
 // Row-staged fused fixed-point step (rows.cuh); eligible when a row of nz
 // float64 is a multiple of 16 bytes and two stages fit in shared memory.

@@ -376,8 +376,9 @@ int imex_create(int nx, int ny, int nz, double tau, double rho0, double u0, int 
 
     const size_t arr = (size_t)kQ * h->ncells * elem_size(precision);
     const size_t nparts = conserved_partials(h->g);
-    // scratch: conserved partials, 5 reduced values, fallback counter, error flag
-    const size_t scratch = nparts * 5 * sizeof(double) + 5 * sizeof(double) + 2 * sizeof(unsigned long long);
+    // scratch: conserved partials, 5 reduced values, fallback counter, error
+    // flag, fixed-point run flag
+    const size_t scratch = nparts * 5 * sizeof(double) + 5 * sizeof(double) + 3 * sizeof(unsigned long long);
     const size_t need = 2 * arr + scratch;
     // Device memory comes from the device's stream-ordered pool: creating
     // and destroying lattices (a server does it per request) then neither
@@ -413,7 +414,8 @@ int imex_create(int nx, int ny, int nz, double tau, double rho0, double u0, int 
     h->d_out = h->d_partial + nparts * 5;
     h->d_fallback = reinterpret_cast<unsigned long long*>(h->d_out + 5);
     h->d_err = reinterpret_cast<unsigned*>(h->d_fallback + 1);
-    e = cudaMemsetAsync(h->d_fallback, 0, 2 * sizeof(unsigned long long), h->stream);
+    h->d_fail = reinterpret_cast<int*>(h->d_fallback + 2);
+    e = cudaMemsetAsync(h->d_fallback, 0, 3 * sizeof(unsigned long long), h->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);  // usable from any stream from here on
     if (e != cudaSuccess) return bail(cuda_fail(nullptr, e, "imex_create"));
     h->bytes = need;
@@ -513,16 +515,83 @@ int imex_streaming(imex_lattice* h)
     return IMEX_OK;
 }
 
-int imex_step(imex_lattice* h, int nsteps)
+}  // extern "C"
+
+namespace {
+
+// The reference's time step (Collision then Streaming), one at a time.
+int step_each(imex_lattice* h, int nsteps)
 {
-    if (nsteps < 0) return fail(h, IMEX_ERR_ARG, "imex_step: nsteps < 0");
     for (int s = 0; s < nsteps; ++s) {
         int rc = imex_collision(h);
         if (rc) return rc;
         rc = imex_streaming(h);
         if (rc) return rc;
     }
-    return check_ready(h, "imex_step");
+    return IMEX_OK;
+}
+
+// n >= 2 steps of the float64 fixed-point engine in the steady state as one
+// run that holds the state as X between its launches (launch_step_fx_run):
+// the same numbers as n fused steps of k_step_fx, 4% faster at 256^3.  A
+// cell leaving the exact range stops the run at that step; the run is then
+// redone from the last complete step by k_step_fx, whose native float64
+// fallback handles such cells.  The run ends with a synchronisation (to read
+// that flag), so it is not used while the stream is being captured.
+int step_fixed_run(imex_lattice* h, int n)
+{
+    const int cur0 = h->cur;
+    const int64_t steps0 = h->steps;
+    IMEX_CUDA(h, cudaMemsetAsync(h->d_fail, 0x7f, sizeof(int), h->stream), "cudaMemset");
+    for (int j = 1; j <= n; ++j) {
+        PhaseScope timed(h->prof, IMEX_PHASE_COLLISION, h->stream);
+        IMEX_CUDA(h, launch_step_fx_run(dbuf(h, h->cur), dbuf(h, 1 - h->cur), h->g, h->fx, j, n, h->d_fail, h->stream),
+                  "step kernel launch");
+        ++h->launches;
+        h->cur = 1 - h->cur;
+        ++h->steps;
+    }
+    int failed = 0;
+    IMEX_CUDA(h, cudaMemcpyAsync(&failed, h->d_fail, sizeof failed, cudaMemcpyDeviceToHost, h->stream), "cudaMemcpy");
+    IMEX_CUDA(h, cudaStreamSynchronize(h->stream), "fixed-point run");
+    if (failed > n) return IMEX_OK;
+    // state after step failed - 1: the source buffer of step `failed`
+    ++h->fx_reruns;
+    h->cur = cur0 ^ ((failed - 1) & 1);
+    h->steps = steps0 + failed - 1;
+    if (failed > 1) IMEX_CUDA(h, launch_fx_to_f64(dbuf(h, h->cur), (size_t)kQ * h->ncells, h->stream), "conversion");
+    return step_each(h, n - failed + 1);
+}
+
+bool capturing(imex_lattice* h)
+{
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    return cudaStreamIsCapturing(h->stream, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone;
+}
+
+}  // namespace
+
+extern "C" {
+
+int imex_step(imex_lattice* h, int nsteps)
+{
+    if (nsteps < 0) return fail(h, IMEX_ERR_ARG, "imex_step: nsteps < 0");
+    int rc = check_ready(h, "imex_step");
+    if (rc) return rc;
+    if (use_fixed(h) && nsteps >= 3) {
+        // reach the steady state (buffer pending a streaming) and the
+        // launch shape, then run the rest as one fixed-point run when the
+        // shape is one thread per cell
+        if (h->tag != kPendingStream) {
+            rc = step_each(h, 1);
+            if (rc) return rc;
+            --nsteps;
+        }
+        rc = ensure_tuned(h);
+        if (rc) return rc;
+        if (h->rows.stages == 0 && !capturing(h)) return step_fixed_run(h, nsteps);
+    }
+    return step_each(h, nsteps);
 }
 
 int imex_conserved(imex_lattice* h, double out[5])

@@ -37,7 +37,7 @@ struct imex_lattice {
     cudaStream_t own_stream = nullptr;
     cudaStream_t stream = nullptr;
     int device = 0;
-    unsigned char* scratch = nullptr;  // one allocation holding the four below
+    unsigned char* scratch = nullptr;  // one allocation holding d_partial .. d_fail
     double* d_partial = nullptr;  // conserved partials (5 per block)
     double* d_out = nullptr;      // 5 reduced values
     unsigned long long* d_fallback = nullptr;  // fixed-point engine fallback counter
@@ -47,6 +47,8 @@ struct imex_lattice {
     FxParams fx{};
     bool fx_ok = false;  // fixed-point engine usable for this lattice
     unsigned* d_err = nullptr;  // set by kernels whose bounded waits ran out
+    int* d_fail = nullptr;      // first failing step of a fixed-point run (imex_step)
+    int64_t fx_reruns = 0;      // fixed-point runs redone from a failing step
     RowConfig rows{};           // launch shape of the fused step (stages 0: one thread per cell)
     int shape_mode = -1;        // -1 autotune on first use, 0 one thread per cell, 1 row-staged
     bool shape_pinned = false;  // shape set by imex_set_launch rather than the autotuner

@@ -163,6 +163,44 @@ def test_set_get_roundtrip_and_restart(imex, oracle):
     assert np.array_equal(a, b)
 
 
+def test_fixed_point_run_equals_single_steps(imex):
+    """imex_step(n) on the fixed-point engine keeps the state as 64-bit fixed
+    point between its launches; single steps go through float64 every step.
+    Both hold the same numbers, so the results are bit-identical."""
+    with imex.LBM(24, 20, 32, 0.003, 1.0, 0.05, engine=imex.IMEX_ENGINE_FIXED) as a, \
+            imex.LBM(24, 20, 32, 0.003, 1.0, 0.05, engine=imex.IMEX_ENGINE_FIXED) as b:
+        for lat in (a, b):
+            lat.set_launch(0, 1, 1)
+            lat.Initialize()
+        a.step(50)
+        for _ in range(50):
+            b.step(1)
+        assert np.array_equal(a.get_f(), b.get_f())
+        assert a.Conserved() == b.Conserved()
+
+
+def test_fixed_point_run_redone_from_failing_step(imex, oracle):
+    """A run whose cells leave the exact range partway (an under-resolved
+    Mach-0.3 deck: the first value leaves [2^-9, 1/8) after ~30 steps) is
+    redone from the last complete step with the per-cell float64 fallback:
+    the result equals stepping one step at a time, bit for bit."""
+    shape, tau, u0, n = (16, 16, 16), 1e-4, 0.18, 40
+    with imex.LBM(*shape, tau, 1.0, u0, engine=imex.IMEX_ENGINE_FIXED) as a, \
+            imex.LBM(*shape, tau, 1.0, u0, engine=imex.IMEX_ENGINE_FIXED) as b:
+        for lat in (a, b):
+            lat.set_launch(0, 1, 1)
+            lat.Initialize()
+        a.step(n)
+        first = None
+        for s in range(1, n + 1):
+            b.step(1)
+            if first is None and b.fallback_cells() > 0:
+                first = s
+        assert first is not None and first >= 3   # the run fails after its first launch
+        assert a.fallback_cells() > 0
+        assert np.array_equal(a.get_f(), b.get_f(), equal_nan=True)
+
+
 def test_nonfinite_is_reported(imex):
     """A diverging request (Mach ~1.7) is reported by status, not a crash."""
     with imex.LBM(16, 16, 16, 1e-4, 1.0, 1.0) as lat:
