@@ -108,7 +108,12 @@ int imex_collision(imex_lattice *h);
 int imex_streaming(imex_lattice *h);
 
 /* Advance nsteps reference steps (Collision then Streaming, repeated).
- * Equivalent to the loop body of src/main.cpp:31-61 without reporting. */
+ * Equivalent to the loop body of src/main.cpp:31-61 without reporting.
+ * On the float64 fixed-point engine, nsteps >= 3 run as one run that keeps
+ * the state in fixed point between its kernel launches (the same numbers,
+ * bit for bit); such a call returns after the run has finished on the
+ * device (it reads whether every cell stayed in the exact range), except
+ * while the handle's stream is being captured. */
 int imex_step(imex_lattice *h, int nsteps);
 
 /* Global diagnostics of the current distributions: out = {mass, px, py, pz,
