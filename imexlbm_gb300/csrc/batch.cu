@@ -112,9 +112,15 @@ __device__ __forceinline__ void batch_cell(const BatchEntry& e, unsigned long lo
 }
 
 // CPT cells per thread, strided by blockDim within a chunk of CPT*blockDim.
-template <int CPT>
-__global__ void __launch_bounds__(256) k_batch(const BatchHeader* __restrict__ hdr, const BatchEntry* __restrict__ tab, int s,
-                                               CollideF32 base)
+// PF = IMEX_F32: every member of the packed index is float32, and only that
+// path is compiled.  With one cell per thread it is held to 64 registers (4
+// CTAs of 256 threads per SM, no spills): at the compiler's 80 only 3 fit,
+// and the kernel, bound by global-load latency, ran at 28.1 GLUPS on the
+// 64-lattice float32 workload (28.7 now; the row kernel, 29.1, stays the
+// autotuner's choice there).
+template <int CPT, int PF>
+__global__ void __launch_bounds__(256, (PF == IMEX_F32 && CPT == 1) ? 4 : 0)
+    k_batch(const BatchHeader* __restrict__ hdr, const BatchEntry* __restrict__ tab, int s, CollideF32 base)
 {
     __shared__ unsigned long long sbegin[kBatchMax + 1];
     const int count = hdr->count;
@@ -136,7 +142,8 @@ __global__ void __launch_bounds__(256) k_batch(const BatchHeader* __restrict__ h
             }
             const BatchEntry& e = tab[lo];
             if (s >= e.steps) continue;
-            if (e.prec == IMEX_F32) batch_cell<IMEX_F32>(e, q - sbegin[lo], s, base);
+            if constexpr (PF == IMEX_F32) batch_cell<IMEX_F32>(e, q - sbegin[lo], s, base);
+            else if (e.prec == IMEX_F32) batch_cell<IMEX_F32>(e, q - sbegin[lo], s, base);
             else batch_cell<IMEX_F16DEV>(e, q - sbegin[lo], s, base);
         }
     }
@@ -234,12 +241,13 @@ struct imex_batch {
     BatchShape shape;
     RowShape rshape;
     int n_cell = 0, n_row = 0;  // members in each kernel (last uploaded table)
+    int n_cell_f16 = 0;         // float16-deviation members in the cell kernel
     int graph_steps = 0;  // K of the captured graph (0: no graph)
     cudaGraphExec_t graph = nullptr;
     int graph_k = 0;
     BatchShape graph_shape;
     RowShape graph_rshape;
-    int graph_kinds = 0;  // bit 0: cell kernel, bit 1: row kernel
+    int graph_kinds = 0;  // bit 0: cell kernel, bit 1: row kernel, bit 2: cell kernel with float16 members
     int64_t launches = 0;
     std::string err;
 };
@@ -285,7 +293,10 @@ bool rows_fit(const RowShape& rs, int members)
     return smem <= 227 * 1024 && (size_t)rs.ctas_per_sm * (smem + 1024) <= 228 * 1024;
 }
 
-int kinds(const imex_batch* b) { return (b->n_cell > 0 ? 1 : 0) | (b->n_row > 0 ? 2 : 0); }
+int kinds(const imex_batch* b)
+{
+    return (b->n_cell > 0 ? 1 : 0) | (b->n_row > 0 ? 2 : 0) | (b->n_cell_f16 > 0 ? 4 : 0);
+}
 
 // One step (index s of the tick) of every member: the cell kernel over its
 // members, then the row kernel over its members.
@@ -294,12 +305,17 @@ cudaError_t launch_step(imex_batch* b, const BatchShape& sh, const RowShape& rs,
     const CollideF32 base = base_constants();
     if (b->n_cell > 0) {
         const dim3 grid((unsigned)(b->sms * sh.ctas_per_sm));
+        const bool f32 = b->n_cell_f16 == 0;
+#define IMEX_BATCH_CELLS(C) \
+    (f32 ? k_batch<C, IMEX_F32><<<grid, sh.threads, 0, b->stream>>>(b->d_hdr, b->d_tab, s, base) \
+         : k_batch<C, 0><<<grid, sh.threads, 0, b->stream>>>(b->d_hdr, b->d_tab, s, base))
         switch (sh.cpt) {
-        case 1: k_batch<1><<<grid, sh.threads, 0, b->stream>>>(b->d_hdr, b->d_tab, s, base); break;
-        case 2: k_batch<2><<<grid, sh.threads, 0, b->stream>>>(b->d_hdr, b->d_tab, s, base); break;
-        case 4: k_batch<4><<<grid, sh.threads, 0, b->stream>>>(b->d_hdr, b->d_tab, s, base); break;
+        case 1: IMEX_BATCH_CELLS(1); break;
+        case 2: IMEX_BATCH_CELLS(2); break;
+        case 4: IMEX_BATCH_CELLS(4); break;
         default: return cudaErrorInvalidValue;
         }
+#undef IMEX_BATCH_CELLS
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }
@@ -357,10 +373,11 @@ int upload_table(imex_batch* b, const std::vector<int>& steps, const RowShape& r
 {
     unsigned long long begin = 0;
     unsigned ibegin = 0;
-    int n = 0, nr = 0;
+    int n = 0, nr = 0, n16 = 0;
     for (size_t m = 0; m < b->members.size(); ++m) {
         imex_lattice* h = b->members[m];
         const int B = rows_per_item(h, rs);
+        if (!B && h->precision != IMEX_F32) ++n16;
         BatchEntry& e = B ? b->h_rtab[nr++] : b->h_tab[n++];
         e.plane = h->ncells;
         e.buf[0] = h->buf[0];
@@ -392,6 +409,7 @@ int upload_table(imex_batch* b, const std::vector<int>& steps, const RowShape& r
     b->h_rhdr->count = nr;
     b->n_cell = n;
     b->n_row = nr;
+    b->n_cell_f16 = n16;
     B_CUDA(b, cudaMemcpyAsync(b->d_tab, b->h_tab, sizeof(BatchEntry) * (n ? n : 1), cudaMemcpyHostToDevice, b->stream),
            "cudaMemcpyAsync");
     B_CUDA(b, cudaMemcpyAsync(b->d_hdr, b->h_hdr, sizeof(BatchHeader), cudaMemcpyHostToDevice, b->stream),
