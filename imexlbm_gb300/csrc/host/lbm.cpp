@@ -65,6 +65,7 @@ void LBM::check(int rc) const { throw_on(rc, h_); }
 void LBM::Initialize() { check(imex_initialize(h_)); }
 void LBM::Collision() { check(imex_collision(h_)); }
 void LBM::Streaming() { check(imex_streaming(h_)); }
+void LBM::Step(int n) { check(imex_step(h_, n)); }
 void LBM::fence() { check(imex_synchronize(h_)); }
 
 void LBM::ComputeMacroscopic(double* p, double* u, double* v, double* w) { check(imex_macroscopic(h_, p, u, v, w)); }

@@ -66,6 +66,10 @@ struct LBM {
     void Initialize();
     void Collision();
     void Streaming();
+    // n reference steps (Collision then Streaming each) in one call: the same
+    // numbers, run as one fixed-point run on the float64 engine (imex_step).
+    // Not in the reference's struct.
+    void Step(int n);
     void ComputeMacroscopic(double* p, double* u, double* v, double* w);
     void Conserved(double& mass, double& mom_x, double& mom_y, double& mom_z, double& ke);
     void MPIoutput(int n);  // lbm.cpp:307-598: writes output<n>.plt

@@ -69,6 +69,16 @@ def test_scaling_build_flag_same_answers(imex, known_answers, tmp_path):
     assert np.array_equal(a, cons_lines(out))
 
 
+def test_runs_between_reports_same_answers(imex, tmp_path):
+    """Without per-step timing the driver runs the steps between report steps
+    as one call (fixed-point runs on the float64 engine): the report lines
+    carry the same numbers as one Collision()/Streaming() pair per step."""
+    deck = "1.0 0.1 1600\n0.05 47 10\n32 32 32\n"
+    a = cons_lines(run_driver(tmp_path, deck))
+    b = cons_lines(run_driver(tmp_path, deck, "--no-perstep-timing"))
+    assert len(a) == 4 and np.array_equal(a, b)
+
+
 def test_missing_deck_fails(imex, tmp_path):
     r = subprocess.run([EXE], cwd=tmp_path, capture_output=True, text=True, timeout=60)
     assert r.returncode == 1 and "cannot open" in r.stderr
