@@ -31,6 +31,10 @@ IMEX_ENGINE_AUTO = 0
 IMEX_ENGINE_NATIVE = 1
 IMEX_ENGINE_FIXED = 2
 
+IMEX_TEST_FAULT_NONE = 0
+IMEX_TEST_FAULT_STARVE_STAGE = 1
+IMEX_TEST_FAULT_BATCH_TABLE = 2
+
 # Every symbol include/imexlbm.h declares, with (restype, argtypes).
 _dp = ctypes.POINTER(ctypes.c_double)
 _h = ctypes.c_void_p
@@ -150,6 +154,7 @@ SIGNATURES = {
     "imex_server_set_policy": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "imex_server_now": (ctypes.c_double, [ctypes.c_void_p]),
     "imex_server_destroy": (None, [ctypes.c_void_p]),
+    "imex_test_set_fault": (ctypes.c_int, [ctypes.c_int, ctypes.c_longlong]),
 }
 
 _lib = None

@@ -155,12 +155,12 @@ __global__ void __launch_bounds__(256, (PF == IMEX_F32 && CPT == 1) ? 4 : 0)
 template <int kDirBytes, int kMinBlocks>
 __global__ void __launch_bounds__(rowslp::kThreads, kMinBlocks)
     k_batch_rows(const RowsHeader* __restrict__ hdr, const BatchEntry* __restrict__ tab, int s, CollideF32 base,
-                 int stages, int table_cap, unsigned* __restrict__ err)
+                 int stages, int table_cap, WaitCtl wc)
 {
     extern __shared__ __align__(128) unsigned char smem[];
     const int count = hdr->count;
     if (count > table_cap) {  // the table would not fit the shared memory the launch has
-        if (threadIdx.x == 0) atomicOr(err, 2u);
+        if (threadIdx.x == 0) atomicOr(wc.err, 2u);
         return;
     }
     const unsigned total = hdr->total;
@@ -200,7 +200,7 @@ __global__ void __launch_bounds__(rowslp::kThreads, kMinBlocks)
         it.active = s < e.steps;
         return it;
     };
-    rowslp::run_items<kDirBytes, lowp::F2, true>(item_of, my, stages, base, smem, err);
+    rowslp::run_items<kDirBytes, lowp::F2, true>(item_of, my, stages, base, smem, wc);
 }
 
 }  // namespace
@@ -326,9 +326,12 @@ cudaError_t launch_step(imex_batch* b, const BatchShape& sh, const RowShape& rs,
         if (!rows_fit(rs, b->capacity)) return cudaErrorInvalidValue;
         const size_t smem = rows_smem(rs, b->capacity);
         const bool one = rs.ctas_per_sm <= 1;  // one resident CTA: the full register file
+        // the test hook IMEX_TEST_FAULT_BATCH_TABLE hands the kernel a table
+        // capacity below the member count, so that its refusal fires
+        const int cap = test_fault_kind() == IMEX_TEST_FAULT_BATCH_TABLE ? b->n_row - 1 : b->capacity;
+        const WaitCtl wc = make_wait_ctl(b->d_err);
 #define IMEX_BATCH_ROWS(D, M) \
-    k_batch_rows<D, M><<<grid, rowslp::kThreads, smem, b->stream>>>(b->d_rhdr, b->d_rtab, s, base, rs.stages, \
-                                                                   b->capacity, b->d_err)
+    k_batch_rows<D, M><<<grid, rowslp::kThreads, smem, b->stream>>>(b->d_rhdr, b->d_rtab, s, base, rs.stages, cap, wc)
         switch (rs.dir_kb) {
         case 1:
             if (one) IMEX_BATCH_ROWS(1024, 1);

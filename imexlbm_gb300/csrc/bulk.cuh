@@ -1,12 +1,27 @@
 // Asynchronous bulk copies global -> shared memory (cp.async.bulk, the
 // non-tensor TMA path) completed on an mbarrier, as inline PTX for sm_103a.
-// Every wait is bounded: after kWaitCycles SM clocks it reports failure and
-// the caller records an error instead of spinning forever.
+// Every wait is bounded: after a limit of SM clocks (WaitCtl::cycles,
+// kWaitCycles unless a test lowers it) it reports failure and the caller
+// records an error instead of spinning forever.
 #pragma once
 
 #include <cstdint>
 
 namespace imex {
+
+// Bounded-wait control handed to every kernel that waits on an mbarrier:
+// where a wait that ran out is recorded (bit 0 of *err), the wait limit in
+// SM clocks, and a test hook - CTA `starve_cta` (-1: none) arms the first
+// stage of its ring without issuing that stage's copies, so its first wait
+// runs out with no copy in flight.  make_wait_ctl (lattice.cu) fills it
+// from the process's test-fault setting (imex_test_set_fault).
+struct WaitCtl {
+    unsigned* err;
+    long long cycles;
+    int starve_cta;
+};
+WaitCtl make_wait_ctl(unsigned* err);
+
 namespace bulk {
 
 constexpr long long kWaitCycles = 1ll << 31;  // ~1 s at 2 GHz
@@ -59,13 +74,13 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
     return done != 0;
 }
 
-// Wait for phase `parity` of bar to complete; false after kWaitCycles.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity)
+// Wait for phase `parity` of bar to complete; false after `cycles` SM clocks.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, long long cycles)
 {
     if (mbar_try_wait(bar, parity)) return true;
     const long long t0 = clock64();
     while (!mbar_try_wait(bar, parity))
-        if (clock64() - t0 > kWaitCycles) return false;
+        if (clock64() - t0 > cycles) return false;
     return true;
 }
 

@@ -34,7 +34,9 @@ std::mutex g_lock;
 double* g_partials_dev[kMaxDevices] = {};
 
 // Device address of g_partials on the current device (looked up on the
-// first call per device).
+// first call per device and kept: a cudaDeviceReset, which unloads the
+// library's device code, would leave the kept address stale - the header
+// tells callers not to use this entry point after a reset).
 int partials_address(double** out)
 {
     int dev = 0;

@@ -11,4 +11,8 @@ namespace imex {
 int set_thread_error(int code, const std::string& msg);
 const char* thread_error();
 
+// The process's test-fault setting (imex_test_set_fault): its kind and value.
+int test_fault_kind();
+long long test_fault_value();
+
 }  // namespace imex

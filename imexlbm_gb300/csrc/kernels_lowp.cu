@@ -260,7 +260,7 @@ cudaError_t launch_rows_lowp_d(int prec, const void* src, void* dst, const Geom&
         if (dev < 64) allowed[dev].store((int)smem);
     }
     rowslp::k_rows_lowp<D, MINB><<<grid, rowslp::kThreads, smem, s>>>(src, dst, g, prec, rc.rows, cp, rc.stages,
-                                                                       err);
+                                                                       make_wait_ctl(err));
     return cudaGetLastError();
 }
 

@@ -15,6 +15,7 @@
 // In the steady state Collision launches one fused kernel and Streaming
 // launches none.  Readers (Conserved, macroscopic, get_f) pull through S
 // when the state is kPending.
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -45,6 +46,27 @@ int set_thread_error(int code, const std::string& msg)
 }
 
 const char* thread_error() { return g_thread_err.c_str(); }
+
+// Test faults (imex_test_set_fault): read at every launch of a kernel with
+// bounded waits; IMEX_TEST_FAULT_NONE in production.
+static std::atomic<int> g_fault_kind{IMEX_TEST_FAULT_NONE};
+static std::atomic<long long> g_fault_value{0};
+
+int test_fault_kind() { return g_fault_kind.load(std::memory_order_relaxed); }
+long long test_fault_value() { return g_fault_value.load(std::memory_order_relaxed); }
+
+WaitCtl make_wait_ctl(unsigned* err)
+{
+    WaitCtl wc;
+    wc.err = err;
+    wc.cycles = bulk::kWaitCycles;
+    wc.starve_cta = -1;
+    if (test_fault_kind() == IMEX_TEST_FAULT_STARVE_STAGE) {
+        wc.cycles = test_fault_value();
+        wc.starve_cta = 0;
+    }
+    return wc;
+}
 
 int lattice_fail(imex_lattice* h, int code, const std::string& msg)
 {
@@ -215,6 +237,46 @@ int time_shape(imex_lattice* h, const RowConfig& rc, int reps, float* ms)
     return IMEX_OK;
 }
 
+// The one-thread-per-cell shape of the float64 fixed-point engine runs, in
+// imex_step's steady state, as k_step_fxs reading and writing X between
+// launches (step_fixed_run), not as k_step_fx: time that form, so that the
+// row shapes are compared with the kernel that would actually run.  One
+// step from the state into the spare buffer gives X on the float64 grid;
+// the timed launches read it and write a temporary third buffer, so the
+// state is untouched.  Without room for the third buffer it times
+// k_step_fx instead.
+int time_fixed_run(imex_lattice* h, int reps, float* ms)
+{
+    const size_t bytes = (size_t)kQ * h->ncells * sizeof(double);
+    double* tmp = nullptr;
+    if (cudaMallocAsync(&tmp, bytes, h->stream) != cudaSuccess) {
+        cudaGetLastError();
+        return time_shape(h, RowConfig{}, reps, ms);
+    }
+    const int n = reps + 2;  // launches 2 .. n-1 read and write X
+    double* x = dbuf(h, 1 - h->cur);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaError_t e = cudaMemsetAsync(h->d_fail, 0x7f, sizeof(int), h->stream);
+    if (e == cudaSuccess) e = launch_step_fx_run(dbuf(h, h->cur), x, h->g, h->fx, 1, n, h->d_fail, h->stream);
+    if (e == cudaSuccess) e = cudaEventCreate(&e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&e1);
+    if (e == cudaSuccess) e = cudaEventRecord(e0, h->stream);
+    for (int r = 0; r < reps && e == cudaSuccess; ++r)
+        e = launch_step_fx_run(x, tmp, h->g, h->fx, 2 + r, n, h->d_fail, h->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(e1, h->stream);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    float t = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&t, e0, e1);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaError_t e2 = cudaFreeAsync(tmp, h->stream);
+    if (e == cudaSuccess) e = e2;
+    if (e != cudaSuccess) return cuda_fail(h, e, "autotune");
+    h->launches += reps + 1;
+    *ms = t / reps;
+    return IMEX_OK;
+}
+
 // Time every candidate in interleaved rounds (so that a drift of the clock
 // or of the memory system during tuning does not favour one candidate) and
 // keep each candidate's fastest round; the fastest candidate wins.
@@ -228,7 +290,8 @@ int tune(imex_lattice* h)
         for (int round = 0; round < 4; ++round)
             for (size_t c = 0; c < cands.size(); ++c) {
                 float ms = 0.f;
-                int rc = time_shape(h, cands[c], round == 0 ? 1 : 4, &ms);  // round 0 warms up
+                const int reps = round == 0 ? 1 : 4;  // round 0 warms up
+                int rc = c == 0 && use_fixed(h) ? time_fixed_run(h, reps, &ms) : time_shape(h, cands[c], reps, &ms);
                 if (rc) return rc;
                 if (round == 1 || ms < fastest[c]) fastest[c] = ms;
             }
@@ -322,20 +385,41 @@ int check_kernel_error(imex_lattice* h)
     return IMEX_OK;
 }
 
-int materialize(imex_lattice* h)
+// Device view of a pinned (page-locked) host buffer, or nullptr for any
+// other pointer (pageable memory is copied through the driver instead).
+double* host_device_view(double* p)
 {
-    if (h->tag != kPendingStream) return IMEX_OK;
-    int rc = launch_mode(h, kModeStream);
-    if (rc) return rc;
-    h->tag = kExact;
-    return IMEX_OK;
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (at.type != cudaMemoryTypeHost || !at.devicePointer) return nullptr;
+    return static_cast<double*>(at.devicePointer);
 }
+
 
 }  // namespace
 
 extern "C" {
 
-const char* imex_version(void) { return "imexlbm-gb300 0.1"; }
+const char* imex_version(void) { return "imexlbm-gb300 0.2"; }
+
+int imex_test_set_fault(int kind, long long value)
+{
+    if (kind == IMEX_TEST_FAULT_NONE) {
+        g_fault_kind.store(kind);
+        g_fault_value.store(0);
+        return IMEX_OK;
+    }
+    if (kind == IMEX_TEST_FAULT_STARVE_STAGE && (value < 1000 || value > bulk::kWaitCycles))
+        return set_thread_error(IMEX_ERR_ARG, "imex_test_set_fault: the wait limit must be in [1000, 2^31] SM clocks");
+    if (kind != IMEX_TEST_FAULT_STARVE_STAGE && kind != IMEX_TEST_FAULT_BATCH_TABLE)
+        return set_thread_error(IMEX_ERR_ARG, "imex_test_set_fault: unknown fault");
+    g_fault_value.store(value);
+    g_fault_kind.store(kind);
+    return IMEX_OK;
+}
 
 const char* imex_last_error(const imex_lattice* h) { return h ? h->err.c_str() : thread_error(); }
 
@@ -705,21 +789,39 @@ static int get_f_impl(imex_lattice* h, double* dst, size_t n, cudaMemcpyKind kin
     if (rc) return rc;
     if (!dst || n != (size_t)kQ * h->ncells) return fail(h, IMEX_ERR_ARG, std::string(what) + ": buffer size must be 27*nx*ny*nz");
     if (is_lowp(h)) {
-        // convert (pulling through a pending streaming) into a float64 buffer
-        double* tmp = dst;
-        if (kind != cudaMemcpyDeviceToDevice)
-            IMEX_CUDA(h, cudaMallocAsync(&tmp, n * sizeof(double), h->stream), "cudaMallocAsync");
+        // convert (pulling through a pending streaming) into a float64
+        // buffer: the destination itself when the device can write it (a
+        // device buffer, or pinned host memory through its device view)
+        double* tmp = kind == cudaMemcpyDeviceToDevice ? dst : host_device_view(dst);
+        const bool staged = tmp == nullptr;
+        if (staged) IMEX_CUDA(h, cudaMallocAsync(&tmp, n * sizeof(double), h->stream), "cudaMallocAsync");
         cudaError_t e = launch_to_f64(h->precision, h->tag == kPendingStream, h->buf[h->cur], h->g, tmp, h->stream);
         if (e == cudaSuccess) ++h->launches;
-        if (e == cudaSuccess && tmp != dst) e = cudaMemcpyAsync(dst, tmp, n * sizeof(double), kind, h->stream);
-        if (tmp != dst) cudaFreeAsync(tmp, h->stream);
+        if (e == cudaSuccess && staged) e = cudaMemcpyAsync(dst, tmp, n * sizeof(double), kind, h->stream);
+        if (staged) cudaFreeAsync(tmp, h->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
         if (e != cudaSuccess) return cuda_fail(h, e, what);
         return IMEX_OK;
     }
-    rc = materialize(h);
-    if (rc) return rc;
-    IMEX_CUDA(h, cudaMemcpyAsync(dst, dbuf(h, h->cur), n * sizeof(double), kind, h->stream), what);
+    if (h->tag != kPendingStream) {
+        IMEX_CUDA(h, cudaMemcpyAsync(dst, dbuf(h, h->cur), n * sizeof(double), kind, h->stream), what);
+        IMEX_CUDA(h, cudaStreamSynchronize(h->stream), what);
+        return IMEX_OK;
+    }
+    // A streaming is pending: one kernel pulls the buffer through S into
+    // the destination - the caller's device buffer, or a pinned host
+    // buffer through its device view (written over the chip-to-chip link,
+    // no staging copy) - and otherwise into the spare buffer, which is
+    // then copied out.  The handle stays pending either way, so the next
+    // fused step (or fixed-point run) proceeds as if nothing was read.
+    double* target = kind == cudaMemcpyDeviceToDevice ? dst : host_device_view(dst);
+    double* out = target ? target : dbuf(h, 1 - h->cur);
+    {
+        PhaseScope timed(h->prof, IMEX_PHASE_STREAM, h->stream);
+        IMEX_CUDA(h, launch_step_f64(kModeStream, dbuf(h, h->cur), out, h->g, h->cf64, h->stream), "stream kernel launch");
+    }
+    ++h->launches;
+    if (!target) IMEX_CUDA(h, cudaMemcpyAsync(dst, out, n * sizeof(double), kind, h->stream), what);
     IMEX_CUDA(h, cudaStreamSynchronize(h->stream), what);
     return IMEX_OK;
 }
@@ -866,7 +968,7 @@ int imex_get_launch(imex_lattice* h, int out[4])
     out[0] = h->rows.stages;
     out[1] = h->rows.stages ? h->rows.rows : 0;
     out[2] = h->rows.ctas_per_sm;
-    out[3] = h->rows.threads;
+    out[3] = h->rows.stages ? h->rows.threads : kStepBlock;  // one thread per cell: blocks of kStepBlock
     return IMEX_OK;
 }
 

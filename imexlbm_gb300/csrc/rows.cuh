@@ -51,7 +51,7 @@ __device__ __forceinline__ int pull_z(int ez, int z, int zm, int zp) { return ez
 template <class E>
 __global__ void __launch_bounds__(kRowThreadsMax, E::kMinBlocks)
     k_rows(const typename E::T* __restrict__ src, typename E::T* __restrict__ dst, Geom g, E eng, int stages, int B,
-           unsigned* __restrict__ err)
+           WaitCtl wc)
 {
     using T = typename E::T;
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -76,6 +76,7 @@ __global__ void __launch_bounds__(kRowThreadsMax, E::kMinBlocks)
     };
     auto issue = [&](int t) {
         if (!issuer) return;
+        if (t == 0 && (int)blockIdx.x == wc.starve_cta) return;  // test hook: stage 0 never fills
         const int item = (int)blockIdx.x + t * G;
         const int x = item / yblocks, y0 = (item - x * yblocks) * B;
         const int a = my_dir;
@@ -109,14 +110,15 @@ __global__ void __launch_bounds__(kRowThreadsMax, E::kMinBlocks)
         // the end of iteration t - 1 released it and thread 0 armed it.
         if (t + stages - 1 < my) issue(t + stages - 1);
         const int s = t % stages;
-        const int ok = bulk::mbar_wait(&full[s], (uint32_t)((t / stages) & 1));
+        const int ok = bulk::mbar_wait(&full[s], (uint32_t)((t / stages) & 1), wc.cycles);
         if (__syncthreads_or(!ok)) {
             // A copy did not complete: record it, wait (bounded) for the
             // copies this CTA still has in flight, and stop.
             if (threadIdx.x == 0) {
-                atomicOr(err, 1u);
+                atomicOr(wc.err, 1u);
                 const int last = t + stages - 1 < my ? t + stages - 1 : my - 1;
-                for (int q = t; q <= last; ++q) bulk::mbar_wait(&full[q % stages], (uint32_t)((q / stages) & 1));
+                for (int q = t; q <= last; ++q)
+                    bulk::mbar_wait(&full[q % stages], (uint32_t)((q / stages) & 1), wc.cycles);
             }
             __syncthreads();
             return;
@@ -171,7 +173,7 @@ cudaError_t launch_rows(const typename E::T* src, typename E::T* dst, const Geom
     const long long items = (long long)g.nx * (g.ny / rc.rows);
     long long grid = (long long)sms * rc.ctas_per_sm;
     if (grid > items) grid = items;
-    k_rows<E><<<(unsigned)grid, rc.threads, smem, s>>>(src, dst, g, eng, rc.stages, rc.rows, err);
+    k_rows<E><<<(unsigned)grid, rc.threads, smem, s>>>(src, dst, g, eng, rc.stages, rc.rows, make_wait_ctl(err));
     return cudaGetLastError();
 }
 

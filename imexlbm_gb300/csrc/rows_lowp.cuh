@@ -199,7 +199,7 @@ __device__ __forceinline__ void compute_item(const unsigned char* __restrict__ i
 // division, cheaper than the shared-memory reads).
 template <int kDirBytes, class Ar, bool kSlots, class ItemOf>
 __device__ __forceinline__ void run_items(const ItemOf& item_of, int my, int stages, const CollideF32& base,
-                                          unsigned char* smem, unsigned* __restrict__ err)
+                                          unsigned char* smem, const WaitCtl& wc)
 {
     constexpr uint32_t kStage = (uint32_t)kQ * kDirBytes;
     uint64_t* full = reinterpret_cast<uint64_t*>(smem);
@@ -220,6 +220,7 @@ __device__ __forceinline__ void run_items(const ItemOf& item_of, int my, int sta
     auto issue = [&](int t) {  // after the barrier that follows arm(t)
         const Item it = kSlots ? slots[t % nslots] : item_of(t);
         if (!it.active) return;
+        if (t == 0 && (int)blockIdx.x == wc.starve_cta) return;  // test hook: stage 0 never fills
         const uint32_t es = elem_bytes(it.prec);
         const uint32_t row_bytes = (uint32_t)it.nz * es;
         const int a = my_dir, B = it.B, ny = it.ny;
@@ -252,14 +253,15 @@ __device__ __forceinline__ void run_items(const ItemOf& item_of, int my, int sta
     for (int t = 0; t < my; ++t) {
         const int s = t % stages;
         if (issuer && t + stages - 1 < my) issue(t + stages - 1);
-        const int ok = bulk::mbar_wait(&full[s], (uint32_t)((t / stages) & 1));
+        const int ok = bulk::mbar_wait(&full[s], (uint32_t)((t / stages) & 1), wc.cycles);
         if (__syncthreads_or(!ok)) {
             // A copy did not complete: record it, wait (bounded) for the
             // copies this CTA still has in flight, and stop.
             if (threadIdx.x == 0) {
-                atomicOr(err, 1u);
+                atomicOr(wc.err, 1u);
                 const int last = t + stages - 1 < my ? t + stages - 1 : my - 1;
-                for (int q = t; q <= last; ++q) bulk::mbar_wait(&full[q % stages], (uint32_t)((q / stages) & 1));
+                for (int q = t; q <= last; ++q)
+                    bulk::mbar_wait(&full[q % stages], (uint32_t)((q / stages) & 1), wc.cycles);
             }
             __syncthreads();
             return;
@@ -280,7 +282,7 @@ __device__ __forceinline__ void run_items(const ItemOf& item_of, int my, int sta
 template <int kDirBytes, int kMinBlocks, class Ar = lowp::F2>
 __global__ void __launch_bounds__(kThreads, kMinBlocks)
     k_rows_lowp(const void* __restrict__ src, void* __restrict__ dst, Geom g, int prec, int B, CollideF32 cp,
-                int stages, unsigned* __restrict__ err)
+                int stages, WaitCtl wc)
 {
     extern __shared__ __align__(128) unsigned char smem[];
     const int yblocks = y_blocks(g.ny, B);
@@ -306,7 +308,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
         it.active = true;
         return it;
     };
-    run_items<kDirBytes, Ar, false>(item_of, my, stages, cp, smem, err);
+    run_items<kDirBytes, Ar, false>(item_of, my, stages, cp, smem, wc);
 }
 
 }  // namespace rowslp

@@ -183,7 +183,10 @@ int imex_checkpoint_load(imex_lattice *h, const char *path);
 
 /* Copy the current distributions (reference order, float64) to the host
  * buffer of n = 27*nx*ny*nz values.  The reference exposes them as the
- * public member LBM::f (src/lbm.hpp:165).  Synchronises. */
+ * public member LBM::f (src/lbm.hpp:165).  A pending streaming is applied
+ * on the way out by one kernel, without changing the handle's state; a
+ * pinned (page-locked) host buffer is written by that kernel directly,
+ * any other through a device staging copy.  Synchronises. */
 int imex_get_f(imex_lattice *h, double *host, size_t n);
 
 /* Overwrite the distributions from a host buffer of n = 27*nx*ny*nz
@@ -209,9 +212,11 @@ int imex_set_f_device(imex_lattice *h, const double *dev, size_t n);
  * Lattices needing more partial sums than that (one per 128 z-cells of a
  * row, e.g. more than 256x256x256) are rejected with IMEX_ERR_ARG.  The
  * first call on each device looks the array's device address up
- * (cudaGetSymbolAddress), so make that first call before any stream
- * capture.  All calls share the array: calls that overlap on the GPU (on
- * different streams, or from different threads) race; serialise them.
+ * (cudaGetSymbolAddress) and keeps it for the process, so make that first
+ * call before any stream capture; a cudaDeviceReset invalidates the kept
+ * address, so do not call this entry point on a device after resetting it.
+ * All calls share the array: calls that overlap on the GPU (on different
+ * streams, or from different threads) race; serialise them.
  * Errors are reported through imex_last_error(NULL). */
 int imex_conserved_noalloc(const double *f_dev, int nx, int ny, int nz, double *out_dev, void *stream);
 
@@ -410,6 +415,30 @@ void imex_server_destroy(imex_server *s);
 
 /* Library version string. */
 const char *imex_version(void);
+
+/* ----------------------------------------------------------- test hooks -- */
+
+/* Make the device-side error paths fire, for tests; no counterpart in the
+ * reference, whose failures abort (src/System.cpp:17-21).  The setting is
+ * process-wide and read at every launch of the row-staged kernels;
+ * IMEX_TEST_FAULT_NONE (the default) restores normal operation.  Neither
+ * fault faults or hangs the GPU: every wait involved is bounded.
+ *   IMEX_TEST_FAULT_STARVE_STAGE  CTA 0 of every row-staged launch
+ *       (imex_set_launch stages >= 2, the batch row kernel) arms the first
+ *       stage of its ring without issuing that stage's copies, and every
+ *       bounded wait gives up after `value` SM clocks (1000 .. 2^31) instead
+ *       of 2^31.  The CTA's first wait runs out, it records the failure,
+ *       waits (bounded) for the copies it has in flight and returns; the next
+ *       synchronising call (imex_conserved, imex_synchronize,
+ *       imex_batch_synchronize) returns IMEX_ERR_CUDA.
+ *   IMEX_TEST_FAULT_BATCH_TABLE   the batch row kernel is launched with a
+ *       member-table capacity one below its member count, so it refuses the
+ *       table; imex_batch_synchronize returns IMEX_ERR_CUDA.
+ * The results of the steps run under a fault are invalid. */
+#define IMEX_TEST_FAULT_NONE 0
+#define IMEX_TEST_FAULT_STARVE_STAGE 1
+#define IMEX_TEST_FAULT_BATCH_TABLE 2
+int imex_test_set_fault(int kind, long long value);
 
 #ifdef __cplusplus
 }

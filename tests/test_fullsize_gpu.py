@@ -68,3 +68,33 @@ def test_reduced_precision_against_float64(imex, name, ke_tol, mass_tol):
     assert abs(got[4] - want[4]) <= ke_tol * want[4]
     assert abs(got[0] - m0) <= mass_tol * m0
     assert du <= 5e-3 * d.u0 and 0.5 * d.u0 < umax < 1.5 * d.u0
+
+
+def test_tuner_pick_matches_direct_timing(imex):
+    """The autotuner compares the row-staged shapes with the one-thread-per-
+    cell shape timed in the form imex_step runs it (a fixed-point run of
+    k_step_fxs, state held as fixed point between launches).  At 256^3 its
+    pick must be, within timing noise, the fastest of all candidates timed
+    directly through imex_step."""
+    import time
+    d = deck(imex)
+    shapes = [(0, 1, 1), (2, 1, 1), (3, 1, 1), (4, 1, 1), (2, 2, 1), (2, 1, 2)]
+    with imex.LBM(N, N, N, d.tau, d.rho0, d.u0, engine=imex.IMEX_ENGINE_FIXED) as lat:
+        lat.Initialize()
+        pick = tuple(lat.get_launch()[:3])
+        lat.step(1)
+        times = {}
+        for rnd in range(2):
+            for sh in shapes:
+                lat.set_launch(*sh)
+                lat.step(4)               # warm-up (and first use of the shape)
+                lat.fence()
+                t0 = time.perf_counter()
+                lat.step(30)
+                lat.fence()
+                dt = time.perf_counter() - t0
+                times[sh] = min(times.get(sh, dt), dt)
+    key = (pick[0], pick[1] if pick[0] else 1, pick[2] if pick[0] else 1)
+    best = min(times.values())
+    assert key in times, (pick, times)
+    assert times[key] <= 1.03 * best, (pick, times)

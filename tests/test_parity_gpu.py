@@ -225,3 +225,53 @@ def test_state_errors(imex):
         assert e.value.code == 6
         with pytest.raises(imex.ImexError):
             lat.get_f(np.empty(10))
+
+
+def test_benchmarked_fixed_point_run_against_oracle(imex, oracle):
+    """The kernel bench.py times: the one-thread-per-cell shape pinned, so
+    that every imex_step(10) of the 32^3 regression deck is a fixed-point
+    run of k_step_fxs (one in-place collision opens the first), checked in
+    every f against the oracle at each report step of src/main.cpp:69-93
+    (every 10 steps, 100 steps)."""
+    d = oracle.parse_deck("1.0 0.1 1600\n0.05 100 10\n32 32 32\n")
+    f = oracle.init(32, 32, 32, d.rho0, d.u0)
+    with imex.LBM(32, 32, 32, d.tau, d.rho0, d.u0, engine=imex.IMEX_ENGINE_FIXED) as lat:
+        lat.set_launch(0, 1, 1)
+        lat.Initialize()
+        assert lat.get_launch()[0] == 0
+        for report in range(1, 11):
+            before = lat.kernel_launches()
+            lat.step(10)
+            # a run of 10 launches: reading f leaves the streaming pending,
+            # so only the first run opens with the in-place collision
+            assert lat.kernel_launches() - before == 10
+            oracle.step(f, d.tau, 10)
+            got = lat.get_f()
+            assert rel_err(got, f) <= RTOL, report
+            c, w = np.array(lat.Conserved()), oracle.conserved(f)
+            assert abs(c[0] - w[0]) <= RTOL * abs(w[0]) and abs(c[4] - w[4]) <= RTOL * abs(w[4])
+        assert lat.fallback_cells() == 0
+        assert lat.steps_done() == 100
+
+
+def test_get_f_leaves_the_streaming_pending(imex):
+    """Reading f pulls through the pending streaming into the destination
+    (pinned host, pageable host or device) without changing the handle:
+    the next step is one fused launch, and the three reads agree."""
+    torch = pytest.importorskip("torch")
+    with imex.LBM(16, 12, 20, 0.01, 1.0, 0.05, engine=imex.IMEX_ENGINE_FIXED) as lat:
+        lat.set_launch(0, 1, 1)
+        lat.Initialize()
+        lat.step(3)
+        n = 27 * 16 * 12 * 20
+        pageable = lat.get_f()
+        pinned = torch.empty(n, dtype=torch.float64, pin_memory=True)
+        lat.get_f(pinned.numpy().reshape(lat.shape))
+        dev = torch.empty(n, dtype=torch.float64, device="cuda")
+        lat.get_f_device(dev.data_ptr(), n)
+        torch.cuda.synchronize()
+        assert np.array_equal(pageable.ravel(), pinned.numpy())
+        assert np.array_equal(pageable.ravel(), dev.cpu().numpy())
+        before = lat.kernel_launches()
+        lat.step(1)
+        assert lat.kernel_launches() - before == 1
