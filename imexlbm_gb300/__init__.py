@@ -11,11 +11,13 @@ Python surface:
 from ._lib import (IMEX_ENGINE_AUTO, IMEX_ENGINE_FIXED, IMEX_ENGINE_NATIVE, IMEX_ERR_ARG, IMEX_ERR_CUDA,
                    IMEX_ERR_DECK, IMEX_ERR_IO, IMEX_ERR_MEMORY, IMEX_ERR_NONFINITE, IMEX_ERR_STATE, IMEX_F16DEV,
                    IMEX_F32, IMEX_F64, IMEX_OK, IMEX_POLICY_ARRIVAL, IMEX_POLICY_LEAST_WORK, IMEX_ROUND_NEAREST,
-                   IMEX_ROUND_STOCHASTIC, ImexError, load)
+                   IMEX_ROUND_STOCHASTIC, IMEX_TEST_FAULT_BATCH_TABLE, IMEX_TEST_FAULT_NONE,
+                   IMEX_TEST_FAULT_STARVE_STAGE, ImexError, load)
 from .lbm import LBM, Batch, Q, Server, System
 
 __all__ = ["System", "LBM", "Batch", "Server", "ImexError", "Q", "load", "IMEX_F64", "IMEX_F32", "IMEX_F16DEV",
            "IMEX_ENGINE_AUTO", "IMEX_ENGINE_NATIVE", "IMEX_ENGINE_FIXED",
            "IMEX_ROUND_NEAREST", "IMEX_ROUND_STOCHASTIC", "IMEX_OK", "IMEX_ERR_ARG", "IMEX_ERR_CUDA",
            "IMEX_ERR_MEMORY", "IMEX_ERR_DECK", "IMEX_ERR_NONFINITE", "IMEX_ERR_STATE", "IMEX_ERR_IO",
-           "IMEX_POLICY_ARRIVAL", "IMEX_POLICY_LEAST_WORK"]
+           "IMEX_POLICY_ARRIVAL", "IMEX_POLICY_LEAST_WORK", "IMEX_TEST_FAULT_NONE", "IMEX_TEST_FAULT_STARVE_STAGE",
+           "IMEX_TEST_FAULT_BATCH_TABLE"]

@@ -26,10 +26,16 @@
  * Layout: f[q][nx][ny][nz], z fastest, interior cells only (the reference's
  * LayoutRight View with its 3 ghost layers stripped).
  *
- * Parity pin: the reference ships no field dumps; its only known answers are
- * the 32^3 kinetic-energy trajectory 9.852 -> 10.219 -> 9.889 after steps 1-3
- * and the mass / momentum invariants (tests/regression.sh:29,41-42).  The
- * CPU test suite checks this oracle against those values.
+ * Parity pin: bit for bit against the reference's own code.  The
+ * reference's unmodified src/*.cpp, built against the single-process
+ * Kokkos / MPI stand-ins of oracle/refshim and run on 1 to 8 ranks,
+ * produce fields whose SHA-256 this oracle reproduces exactly (32^3 and
+ * 18x20x22 decks, 20-100 steps), `cons` lines it matches to the rounding of
+ * the summation order, and a Tecplot file this writer reproduces byte for
+ * byte (tests/golden/reference_runs.json, tests/test_reference_pin.py).
+ * It also meets the reference's published known answers: the 32^3
+ * kinetic-energy trajectory 9.852 -> 10.219 -> 9.889 after steps 1-3 and
+ * the mass / momentum invariants (tests/regression.sh:29,41-42).
  */
 #include <math.h>
 #include <stdint.h>

@@ -155,3 +155,62 @@ def write_tecplot(f: np.ndarray, n: int, path: str) -> None:
     _, nx, ny, nz = f.shape
     if lib().oracle_write_tecplot(nx, ny, nz, _p(f), int(n), str(path).encode()) != 0:
         raise OSError(f"cannot write {path}")
+
+
+# ---------------------------------------------------------------------------
+# The reference's own code (oracle/_ref/imexref): its unmodified src/*.cpp
+# built against the single-process Kokkos / MPI stand-ins of oracle/refshim
+# by `make -C oracle ref` (see oracle/Makefile).  Test infrastructure, like
+# the rest of this module.
+
+REF_EXE = os.path.join(HERE, "_ref", os.uname().machine, "imexref")
+REF_SRC_DEFAULT = "/root/reference/src"
+
+
+def build_ref(refsrc: str | None = None) -> str | None:
+    """Build oracle/_ref/imexref from the reference's sources (REFSRC, or the
+    copy staged in oracle/_ref/src).  Returns its path, or None when neither
+    source is present."""
+    src = refsrc or os.environ.get("IMEXREF_SRC", REF_SRC_DEFAULT)
+    staged = os.path.join(HERE, "_ref", "src", "lbm.cpp")
+    if not os.path.isdir(src) and not os.path.exists(staged):
+        return None
+    subprocess.run(["make", "-s", "-C", HERE, "ref", f"REFSRC={src}", "-j", str(min(8, os.cpu_count() or 1))],
+                   check=True, stdout=subprocess.DEVNULL)
+    return REF_EXE if os.path.exists(REF_EXE) else None
+
+
+def run_ref(deck: str, cwd: str, ranks: int = 1, threads: int | None = None, mode: str = "main",
+            args: tuple = (), timeout: float = 600.0) -> str:
+    """Run the reference's code on `ranks` rank threads in directory cwd
+    (which gets the deck as input.in); returns its standard output."""
+    with open(os.path.join(cwd, "input.in"), "w") as fp:
+        fp.write(deck)
+    cmd = [REF_EXE, "--ranks", str(ranks)]
+    if threads:
+        cmd += ["--threads", str(threads)]
+    cmd += [mode, *map(str, args)]
+    r = subprocess.run(cmd, cwd=cwd, capture_output=True, text=True, timeout=timeout)
+    if r.returncode != 0:
+        raise RuntimeError(f"imexref failed ({r.returncode}): {r.stderr[-2000:]}")
+    return r.stdout
+
+
+def parse_cons(text: str) -> list:
+    """The `cons` lines of src/main.cpp:88-93: [(step, mass, px, py, pz, ke)]."""
+    out = []
+    for ln in text.splitlines():
+        if ln.startswith("cons"):
+            parts = [p for p in ln.replace("|", " ").split() if p]
+            out.append((int(parts[2]), float(parts[4]), float(parts[6]), float(parts[8]), float(parts[10]),
+                        float(parts[12])))
+    return out
+
+
+def parse_mlups(text: str) -> list:
+    """The MLUPS figures of the `step` lines of src/main.cpp:75-80."""
+    out = []
+    for ln in text.splitlines():
+        if ln.startswith("step") and ln.rstrip().endswith("MLUPS"):
+            out.append(float(ln.split("|")[-1].split()[0]))
+    return out

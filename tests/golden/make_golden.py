@@ -9,7 +9,7 @@ mounted; the GPU machine never reads the reference) and writes:
                                   measured residual scale of tests/regression.sh
   shipped_deck.json               the shipped input.in text and its nine fields
 
-Usage: python tests/golden/make_golden.py [/path/to/reference]
+Usage: python tests/golden/make_golden.py /path/to/reference
 """
 from __future__ import annotations
 
@@ -72,4 +72,6 @@ def main(ref: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        raise SystemExit(__doc__)
+    main(sys.argv[1])

@@ -97,8 +97,9 @@ def test_batch_table_refusal_is_reported(imex, fault):
             batch.add(lat)
         batch.set_graph(0)
         batch.set_row_launch(2, 2, 1, True)
+        batch.step(1)                    # first collisions run alone, in place
         fault(imex.IMEX_TEST_FAULT_BATCH_TABLE)
-        batch.step(1)
+        batch.step(2)
         with pytest.raises(imex.ImexError) as e:
             batch.synchronize()
         assert e.value.code == imex.IMEX_ERR_CUDA
