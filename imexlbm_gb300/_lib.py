@@ -93,6 +93,29 @@ class ServerStats(ctypes.Structure):
                 ("busy_seconds", ctypes.c_double), ("now", ctypes.c_double), ("failed", ctypes.c_int64)]
 
 
+class Block(ctypes.Structure):
+    """struct imex_block (include/imexlbm.h)."""
+
+    _fields_ = [("rank", ctypes.c_int), ("coord", ctypes.c_int * 3), ("lo", ctypes.c_int * 3),
+                ("len", ctypes.c_int * 3)]
+
+
+class HaloMsg(ctypes.Structure):
+    """struct imex_halo_msg (include/imexlbm.h)."""
+
+    _fields_ = [("channel", ctypes.c_int), ("offset", ctypes.c_int * 3), ("send_to", ctypes.c_int),
+                ("recv_from", ctypes.c_int), ("send_lo", ctypes.c_int * 3), ("recv_lo", ctypes.c_int * 3),
+                ("ext", ctypes.c_int * 3), ("ndir", ctypes.c_int), ("dirs", ctypes.c_int * 9)]
+
+
+class DomainStats(ctypes.Structure):
+    """struct imex_domain_stats (include/imexlbm.h)."""
+
+    _fields_ = [("nranks", ctypes.c_int), ("grid", ctypes.c_int * 3), ("steps", ctypes.c_int64),
+                ("launches", ctypes.c_int64), ("halo_values_per_step", ctypes.c_int64),
+                ("device_bytes", ctypes.c_int64)]
+
+
 SIGNATURES = {
     "imex_deck_parse": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(Deck)]),
     "imex_deck_read": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(Deck)]),
@@ -155,6 +178,24 @@ SIGNATURES = {
     "imex_server_now": (ctypes.c_double, [ctypes.c_void_p]),
     "imex_server_destroy": (None, [ctypes.c_void_p]),
     "imex_test_set_fault": (ctypes.c_int, [ctypes.c_int, ctypes.c_longlong]),
+    "imex_decomp_grid": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                        ctypes.POINTER(ctypes.c_int)]),
+    "imex_decomp_block": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                         ctypes.POINTER(Block)]),
+    "imex_decomp_halo": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                        ctypes.c_int, ctypes.POINTER(HaloMsg)]),
+    "imex_domain_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                          ctypes.c_double, ctypes.c_double, ctypes.POINTER(ctypes.c_void_p)]),
+    "imex_domain_destroy": (None, [ctypes.c_void_p]),
+    "imex_domain_initialize": (ctypes.c_int, [ctypes.c_void_p]),
+    "imex_domain_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "imex_domain_conserved": (ctypes.c_int, [ctypes.c_void_p, _dp]),
+    "imex_domain_conserved_blocks": (ctypes.c_int, [ctypes.c_void_p, _dp]),
+    "imex_domain_get_f": (ctypes.c_int, [ctypes.c_void_p, _dp, ctypes.c_size_t]),
+    "imex_domain_info": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(DomainStats)]),
+    "imex_domain_fallback_cells": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64)]),
+    "imex_domain_synchronize": (ctypes.c_int, [ctypes.c_void_p]),
+    "imex_domain_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
 }
 
 _lib = None

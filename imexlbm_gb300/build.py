@@ -34,7 +34,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
           "-I", INCLUDE, "-I", CSRC]
 # Sources of the shared library.
-LIB_SOURCES = ["lattice.cu", "kernels_f64.cu", "kernels_fx.cu", "kernels_lowp.cu", "fx_params.cpp", "deck.cpp", "conserved_noalloc.cu", "batch.cu", "server.cu", "fields.cu"]
+LIB_SOURCES = ["lattice.cu", "kernels_f64.cu", "kernels_fx.cu", "kernels_lowp.cu", "fx_params.cpp", "deck.cpp",
+               "conserved_noalloc.cu", "batch.cu", "server.cu", "fields.cu", "decomp.cu"]
 # Sources of the driver executable (host C++ facade + main).
 EXE_SOURCES = ["lbm.cpp", "main.cpp"]
 

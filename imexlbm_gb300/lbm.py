@@ -290,6 +290,109 @@ class Batch:
         self.close()
 
 
+def decomp_grid(nranks: int, nx: int, ny: int, nz: int):
+    """The reference's rank grid (rx, ry, rz) for nranks ranks
+    (setup_Cartesian, src/mpi_view_transfer.cpp:53-95)."""
+    L = _lib.load()
+    out = (ctypes.c_int * 3)()
+    check(L.imex_decomp_grid(int(nranks), int(nx), int(ny), int(nz), out))
+    return tuple(out)
+
+
+def decomp_block(nranks: int, nx: int, ny: int, nz: int, rank: int) -> dict:
+    """Rank `rank`'s block: coord (px, py, pz), lo and len per axis."""
+    L = _lib.load()
+    b = _lib.Block()
+    check(L.imex_decomp_block(int(nranks), int(nx), int(ny), int(nz), int(rank), ctypes.byref(b)))
+    return {"rank": b.rank, "coord": tuple(b.coord), "lo": tuple(b.lo), "len": tuple(b.len)}
+
+
+def decomp_halo(nranks: int, nx: int, ny: int, nz: int, rank: int, channel: int) -> dict:
+    """Halo channel `channel` (0..25) of rank `rank`: peers, boxes in padded
+    block coordinates and the directions it carries."""
+    L = _lib.load()
+    m = _lib.HaloMsg()
+    check(L.imex_decomp_halo(int(nranks), int(nx), int(ny), int(nz), int(rank), int(channel), ctypes.byref(m)))
+    return {"channel": m.channel, "offset": tuple(m.offset), "send_to": m.send_to, "recv_from": m.recv_from,
+            "send_lo": tuple(m.send_lo), "recv_lo": tuple(m.recv_lo), "ext": tuple(m.ext),
+            "dirs": tuple(m.dirs[:m.ndir])}
+
+
+class Domain:
+    """A lattice decomposed into `nranks` blocks on this GPU, stepped as the
+    reference's ranks step theirs (include/imexlbm.h, imex_domain_*)."""
+
+    def __init__(self, sx: int, sy: int, sz: int, nranks: int, tau: float, rho0: float, u0: float):
+        self._L = _lib.load()
+        d = ctypes.c_void_p()
+        check(self._L.imex_domain_create(int(sx), int(sy), int(sz), int(nranks), float(tau), float(rho0), float(u0),
+                                         ctypes.byref(d)))
+        self._d = d
+        self.glx, self.gly, self.glz = int(sx), int(sy), int(sz)
+        self.nranks = int(nranks)
+
+    def _check(self, rc: int) -> None:
+        if rc != _lib.IMEX_OK:
+            msg = self._L.imex_domain_last_error(self._d)
+            raise ImexError(rc, msg.decode() if msg else "")
+
+    @property
+    def shape(self):
+        return (Q, self.glx, self.gly, self.glz)
+
+    def Initialize(self) -> None:
+        self._check(self._L.imex_domain_initialize(self._d))
+
+    def step(self, n: int = 1) -> None:
+        self._check(self._L.imex_domain_step(self._d, int(n)))
+
+    def Conserved(self):
+        out = (ctypes.c_double * 5)()
+        self._check(self._L.imex_domain_conserved(self._d, out))
+        return tuple(out)
+
+    def conserved_blocks(self) -> np.ndarray:
+        out = np.zeros((self.nranks, 5))
+        self._check(self._L.imex_domain_conserved_blocks(self._d, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+        return out
+
+    def get_f(self) -> np.ndarray:
+        f = np.empty(self.shape)
+        self._check(self._L.imex_domain_get_f(self._d, f.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), f.size))
+        return f
+
+    def info(self) -> dict:
+        st = _lib.DomainStats()
+        self._check(self._L.imex_domain_info(self._d, ctypes.byref(st)))
+        return {"nranks": st.nranks, "grid": tuple(st.grid), "steps": st.steps, "launches": st.launches,
+                "halo_values_per_step": st.halo_values_per_step, "device_bytes": st.device_bytes}
+
+    def fallback_cells(self) -> int:
+        v = ctypes.c_int64()
+        self._check(self._L.imex_domain_fallback_cells(self._d, ctypes.byref(v)))
+        return int(v.value)
+
+    def fence(self) -> None:
+        self._check(self._L.imex_domain_synchronize(self._d))
+
+    def close(self) -> None:
+        if getattr(self, "_d", None):
+            self._L.imex_domain_destroy(self._d)
+            self._d = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
 class Server:
     """Request server with continuous batching (include/imexlbm.h,
     imex_server_*): submit solves from any thread, poll finished results."""

@@ -413,6 +413,88 @@ int imex_server_set_policy(imex_server *s, int policy);
 /* Stop the server thread; requests still queued or running are dropped. */
 void imex_server_destroy(imex_server *s);
 
+/* -------------------------------------------------------- decomposition -- */
+
+/* Spatial decomposition of one lattice into blocks, the reference's
+ * multi-rank layout (src/mpi_view_transfer.cpp), with the halo pruned to
+ * the directions that cross each channel.  The plan calls below are host
+ * arithmetic (no GPU); a multi-rank host code can exchange the messages
+ * they describe over its own transport. */
+
+/* One rank's block: rank = coord[0] + rx*coord[2] + rx*rz*coord[1]
+ * (src/mpi_view_transfer.cpp:97-99), cells lo .. lo+len-1 per axis
+ * (setup_Local's block distribution, :163-195). */
+typedef struct imex_block {
+    int rank;
+    int coord[3]; /* px, py, pz */
+    int lo[3];    /* first global cell per axis */
+    int len[3];   /* cells per axis */
+} imex_block;
+
+/* One of a rank's 26 halo channels, in the reference's order (faces left,
+ * right, down, up, front, back; 12 edges; 8 corners;
+ * src/mpi_view_transfer.cpp:101-161).  The rank sends its boundary box on
+ * side `offset` to send_to and receives the box of ghost cells on side
+ * -offset from recv_from.  Boxes are in padded block coordinates: 1..len
+ * interior, 0 and len+1 the one-cell ghost shell.  The message carries only
+ * the directions e_a that cross the channel (e_a equal to offset on its
+ * non-zero axes): 9 for a face, 3 for an edge, 1 for a corner, in
+ * reference order; ndir * ext[0] * ext[1] * ext[2] values. */
+typedef struct imex_halo_msg {
+    int channel;
+    int offset[3];
+    int send_to, recv_from;
+    int send_lo[3], recv_lo[3], ext[3];
+    int ndir;
+    int dirs[9]; /* -1 past ndir */
+} imex_halo_msg;
+
+/* The rank grid {rx, ry, rz} of setup_Cartesian (src/mpi_view_transfer.cpp:
+ * 53-95): among the factorisations of nranks in ascending (rx, ry) order,
+ * the first whose integer block extents have the least spread.  Refuses
+ * grids with more ranks than cells along an axis. */
+int imex_decomp_grid(int nranks, int nx, int ny, int nz, int grid[3]);
+int imex_decomp_block(int nranks, int nx, int ny, int nz, int rank, imex_block *out);
+int imex_decomp_halo(int nranks, int nx, int ny, int nz, int rank, int channel, imex_halo_msg *out);
+
+/* A lattice decomposed into nranks blocks held on the current GPU, stepped
+ * as the reference's ranks step theirs (no counterpart as one object: the
+ * reference runs one block per MPI rank).  Each block keeps float64
+ * distributions in a padded box with a one-cell ghost shell; a step is one
+ * halo-exchange kernel for all blocks (the pruned messages above, read from
+ * the neighbours' memory) and one fused pull + collision kernel per block
+ * (the fixed-point engine's arithmetic, so 0.75 <= rho0 <= 1.25).  Every f
+ * equals the undivided lattice's bit for bit; the conserved sums are the
+ * blocks' sums added in rank order. */
+typedef struct imex_domain imex_domain;
+typedef struct imex_domain_stats {
+    int nranks;
+    int grid[3];
+    int64_t steps, launches;
+    int64_t halo_values_per_step; /* values the halo exchange moves per step */
+    int64_t device_bytes;
+} imex_domain_stats;
+
+int imex_domain_create(int nx, int ny, int nz, int nranks, double tau, double rho0, double u0, imex_domain **out);
+void imex_domain_destroy(imex_domain *d);
+/* Taylor-Green initial field of each block at its global coordinates
+ * (LBM::Initialize on every rank, src/lbm.cpp:38-111). */
+int imex_domain_initialize(imex_domain *d);
+/* nsteps reference steps (Collision then Streaming) of every block. */
+int imex_domain_step(imex_domain *d, int nsteps);
+/* out = {mass, px, py, pz, ke}: each block's sums, added in rank order
+ * (LBM::Conserved's MPI_Allreduce, src/lbm.cpp:266-306).  Synchronises. */
+int imex_domain_conserved(imex_domain *d, double out[5]);
+/* The same per block: out[5 * rank + q]. */
+int imex_domain_conserved_blocks(imex_domain *d, double *out);
+/* The whole lattice's f (reference order, n = 27*nx*ny*nz) gathered from
+ * the blocks.  Synchronises. */
+int imex_domain_get_f(imex_domain *d, double *host, size_t n);
+int imex_domain_info(const imex_domain *d, imex_domain_stats *out);
+int imex_domain_fallback_cells(imex_domain *d, int64_t *out);
+int imex_domain_synchronize(imex_domain *d);
+const char *imex_domain_last_error(const imex_domain *d);
+
 /* Library version string. */
 const char *imex_version(void);
 
