@@ -63,6 +63,8 @@ def parse_args(argv=None):
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--launch", default=None, metavar="STAGES,ROWS,CTAS",
                     help="pin the fused step's launch shape instead of autotuning it (stages 0: one thread per cell)")
+    ap.add_argument("--quick", action="store_true",
+                    help="skip the precision sweep, batched and served workloads (added to the line by default)")
     return ap.parse_args(argv)
 
 
@@ -272,6 +274,91 @@ def workload_config(a, engine):
             "parallelism": "replicas (one independent lattice per GPU)"}
 
 
+# ------------------------------------------------- the other configurations --
+def extended_precision(hbm: float):
+    """Precision sweep: 512^3 Taylor-Green, Re 1600, u0 0.05, 2000 steps,
+    float64 against float32 and float16 deviations (nearest and stochastic
+    rounding), all resident at once; errors against the float64 run at every
+    500 steps."""
+    from imexlbm_gb300 import sweep
+    r = sweep.run(size=512, steps=2000, report=500, log=lambda _: None)
+    bpc = {"f64": 432, "f32": 216, "f16dev": 108, "f16dev_sr": 108}
+    out = {"workload": "taylor-green 512^3, Re=1600, u0=0.05, 2000 steps, errors vs the float64 run every 500 steps",
+           "runs": {}}
+    for name, mlups in r["mlups"].items():
+        achieved = mlups * 1e6 * bpc[name] / 1e9
+        run = {"glups": round(mlups / 1e3, 3), "bytes_per_cell": bpc[name], "roofline_frac": round(achieved / hbm, 4)}
+        if name in r["worst"]:
+            w = r["worst"][name]
+            run.update({"ke_rel_err_max": w["ke_rel"], "u_max_err_over_u0": w["u_max_over_u0"],
+                        "mass_drift_rel_max": w["mass_drift_rel"]})
+        out["runs"][name] = run
+    out["f64_fallback_cells"] = r["f64_fallback_cells"]
+    return out
+
+
+def extended_batched():
+    """64 uneven float32 lattices (edges 32-128, seeded), 500 steps in the
+    batch kernels against the plain float64 path on the same lattices."""
+    from imexlbm_gb300 import batched
+    r = batched.run(n=64, steps=500, precision="f32", log=lambda _: None)
+    return {"workload": "64 taylor-green lattices, edges {32,48,64,96,128}, Re U[100,3200], u0 U[0.02,0.08], "
+                        "random phases, seed 20261203, 500 steps, float32 storage",
+            "glups": round(r["batch_mlups"] / 1e3, 3), "fp64_plain_glups": round(r["fp64_plain_mlups"] / 1e3, 3),
+            "multiple_of_fp64_plain": round(r["speedup_vs_fp64_plain"], 3), "ke_rel_err_max": r["ke_rel_err_max"],
+            "mass_drift_max": r["mass_drift_max"], "cells": r["cells"], "row_launch": list(r["row_launch"]),
+            "cell_launch": list(r["launch_shape"])}
+
+
+def extended_served():
+    """The served trace: Poisson arrivals at 50 requests/s for 60 s into the
+    continuous-batching server (120 GB budget), float32 / float16-deviation
+    solves, 16 float64 spot checks."""
+    from imexlbm_gb300 import serve
+    r = serve.run(rate=50.0, duration=60.0, budget_gb=120.0, spot=16, log=lambda _: None)
+    keys = ("requests", "completed", "diverged", "failed", "unfinished", "ttr_p50_s", "ttr_p99_s", "ttr_max_s",
+            "aggregate_mlups", "busy_mlups", "fp64_plain_mlups_on_sample", "aggregate_vs_fp64_plain",
+            "ke_rel_err_vs_f64_max", "ke_rel_err_vs_f64_median", "spot_checks", "alone_equals_mix",
+            "diverged_checked", "diverged_also_in_f64", "peak_active", "offered_lups")
+    out = {"workload": "poisson 50 req/s for 60 s, edges {32..256} weighted, Re log-U[100,5000], u0 U[0.02,0.08], "
+                       "steps U[200,5000], f32/f16dev 50/50, 120 GB budget, seed 20261203"}
+    out.update({k: r.get(k) for k in keys})
+    return out
+
+
+def run_extended(hbm: float):
+    out = {}
+    for key, fn in (("precision", lambda: extended_precision(hbm)), ("batched", extended_batched),
+                    ("served", extended_served)):
+        t0 = time.perf_counter()
+        try:
+            out[key] = fn()
+        except Exception as e:  # keep the main measurement; say what failed
+            out[key] = {"error": f"{type(e).__name__}: {e}"}
+        out[key]["wall_s"] = round(time.perf_counter() - t0, 1)
+    return out
+
+
+def pinned_copy_gbs(nbytes: int, stream):
+    """One plain pinned-host <-> device copy of nbytes each way (torch's
+    copy_ is a cudaMemcpyAsync), best of three: the link the e2e copies use."""
+    import torch
+    host = torch.empty(nbytes // 8, dtype=torch.float64, pin_memory=True)
+    dev = torch.empty(nbytes // 8, dtype=torch.float64, device="cuda")
+    best = {"h2d": 0.0, "d2h": 0.0}
+    with torch.cuda.stream(stream):
+        for _ in range(3):
+            for key, (dst, src) in (("h2d", (dev, host)), ("d2h", (host, dev))):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                dst.copy_(src, non_blocking=True)
+                e1.record(stream)
+                e1.synchronize()
+                best[key] = max(best[key], nbytes / (e0.elapsed_time(e1) * 1e-3) / 1e9)
+    del host, dev
+    return {"pinned_h2d_gbs": round(best["h2d"], 1), "pinned_d2h_gbs": round(best["d2h"], 1)}
+
+
 # ------------------------------------------------------------------ GPU arm --
 def run_ours(a):
     import numpy as np
@@ -385,8 +472,10 @@ def run_ours(a):
                "h2d_bytes_per_step": round(nval * 8 / a.steps, 1),
                "d2h_bytes_per_step": round((nval * 8 + 40 * reports) / a.steps, 1),
                "what": f"imex_set_f from pinned host, {a.steps} steps with imex_conserved every "
-                       f"{a.report_every}, imex_get_f to pinned host"}
+                       f"{a.report_every}, imex_get_f to pinned host (a pending streaming is applied by the "
+                       f"kernel that writes the pinned buffer)"}
         del host
+        e2e.update(pinned_copy_gbs(nval * 8, stream))
 
     cpu = None
     if rank == 0 and world == 1 and not a.no_cpu_baseline:
@@ -398,6 +487,8 @@ def run_ours(a):
         cpu = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
 
     lat.close()
+    extended = run_extended(hbm) if (rank == 0 and world == 1 and not a.quick and a.size == 256
+                                     and a.precision == "f64") else None
     if rank == 0:
         line = {"metric": "MLUPS", "value": round(value, 2), "unit": "MLUPS", "n_gpus": world, "steps": a.steps,
                 "warmup": max(3, a.warmup), "ms_per_step": round(t_max / a.steps, 4), "higher_is_better": True,
@@ -412,6 +503,8 @@ def run_ours(a):
                 "gpu_launches": gpu_launches, "clocks": clk.summary(),
                 "fallback_cells": fallback, "mass": cons[0], "ke": cons[4],
                 "roofline_glups_at_peak": round(hbm / bpc, 3)}
+        if extended:
+            line.update(extended)
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist

@@ -133,6 +133,7 @@ SIGNATURES = {
     "imex_profile_enable": (ctypes.c_int, [_h, ctypes.c_int]),
     "imex_profile_read": (ctypes.c_int, [_h, ctypes.c_void_p, ctypes.c_int]),
     "imex_write_tecplot": (ctypes.c_int, [_h, ctypes.c_char_p, ctypes.c_int]),
+    "imex_write_output": (ctypes.c_int, [_h, ctypes.c_char_p, ctypes.c_int]),
     "imex_checkpoint_save": (ctypes.c_int, [_h, ctypes.c_char_p]),
     "imex_checkpoint_load": (ctypes.c_int, [_h, ctypes.c_char_p]),
     "imex_get_f": (ctypes.c_int, [_h, _dp, ctypes.c_size_t]),

@@ -266,18 +266,28 @@ __global__ void __launch_bounds__(kThreads) k_dom_init(double* __restrict__ f, P
     for (int a = 0; a < kQ; ++a) f[(size_t)a * b.plane + c] = fe[a];
 }
 
-// In-place collision of the interior in native float64 (the first
-// Collision() of a run, as the undivided lattice does it).
-__global__ void __launch_bounds__(kThreads) k_dom_collide(double* __restrict__ f, PadGeom b, CollideF64 cp)
+// In-place collision of the interior (the first Collision() of a run), with
+// the undivided lattice's arithmetic: fixed point, native float64 for a
+// cell outside its exact range.
+template <bool OM_GE1>
+__global__ void __launch_bounds__(kThreads, 5) k_dom_collide(double* __restrict__ f, PadGeom b, FxConst c,
+                                                            CollideF64 cp, unsigned long long* __restrict__ fallback)
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, i = blockIdx.z;
     if (k >= b.L[2]) return;
-    double v[kQ];
+    double v[kQ], out[kQ];
     load_cell(f, b, i + 1, j + 1, k + 1, v);
-    collide_f64(v, cp);
-    const size_t c = pad_index(b, i + 1, j + 1, k + 1);
+    bool ok = true;
+    fx::collide_cell<OM_GE1>(v, out, c, ok);
+    if (!ok) {
+        collide_f64(v, cp);
 #pragma unroll
-    for (int a = 0; a < kQ; ++a) f[(size_t)a * b.plane + c] = v[a];
+        for (int a = 0; a < kQ; ++a) out[a] = v[a];
+        atomicAdd(fallback, 1ull);
+    }
+    const size_t cell = pad_index(b, i + 1, j + 1, k + 1);
+#pragma unroll
+    for (int a = 0; a < kQ; ++a) f[(size_t)a * b.plane + cell] = out[a];
 }
 
 // Native float64 redo of one cell outside the fixed-point range.
@@ -442,12 +452,17 @@ int halo(imex_domain* d)
     return IMEX_OK;
 }
 
-// First Collision of a run: in place, native float64, the streaming then
-// pending (the undivided lattice's imex_collision on an exact state).
+// First Collision of a run: in place, the streaming then pending (the
+// undivided lattice's imex_collision on an exact state).
 int collide_exact(imex_domain* d)
 {
     for (const BlockDev& b : d->dev) {
-        k_dom_collide<<<block_grid(b), kThreads, 0, d->stream>>>(b.buf[d->cur], b.g, d->cf64);
+        if (d->fx.om_ge1)
+            k_dom_collide<true><<<block_grid(b), kThreads, 0, d->stream>>>(b.buf[d->cur], b.g, d->fx.k, d->cf64,
+                                                                          d->d_fallback);
+        else
+            k_dom_collide<false><<<block_grid(b), kThreads, 0, d->stream>>>(b.buf[d->cur], b.g, d->fx.k, d->cf64,
+                                                                           d->d_fallback);
         D_CUDA(d, cudaGetLastError(), "collision kernel launch");
         ++d->launches;
     }
@@ -537,6 +552,7 @@ int imex_domain_create(int nx, int ny, int nz, int nranks, double tau, double rh
     int rc = check_plan_args(nranks, nx, ny, nz, "imex_domain_create", &p);
     if (rc) return rc;
     if (nranks > 512) return set_thread_error(IMEX_ERR_ARG, "imex_domain_create: at most 512 sub-domains");
+    if (nx > 65535 || ny > 65535) return set_thread_error(IMEX_ERR_ARG, "imex_domain_create: nx and ny must be <= 65535");
     if (!std::isfinite(tau) || !std::isfinite(rho0) || !std::isfinite(u0) || !(tau + 0.5 > 0.0))
         return set_thread_error(IMEX_ERR_ARG, "imex_domain_create: tau, rho0, u0 must be finite with tau > -0.5");
     imex_domain* d = new imex_domain();

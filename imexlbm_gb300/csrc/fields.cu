@@ -1,12 +1,14 @@
 // Field output and the min/max report diagnostics:
 //   imex_minmax_uvwp      the "minmax_uvwp" reduction of LBM::MPIoutput
 //                         (src/lbm.cpp:351-372)
+//   imex_write_output     LBM::Output on one rank (src/lbm.cpp:606-636): the
+//                         ASCII dump of f(0)
 //   imex_write_tecplot    LBM::MPIoutput on one rank (src/lbm.cpp:307-598):
 //                         a binary Tecplot file of x, y, z, u, v, w, p
 //   imex_checkpoint_save  the handle's raw device state to a file, and
 //   imex_checkpoint_load  back (no reference counterpart)
 //
-// One kernel serves the first two: per cell it forms p = sum f / 3 and
+// One kernel serves the min/max and the Tecplot file: per cell it forms p = sum f / 3 and
 // u = sum f e (the ComputeMacroscopic moments, src/lbm.cpp:218-236, pulled
 // through a pending streaming), reduces their minima and maxima, and - for
 // the file - writes the four fields transposed to the file's x-fastest
@@ -413,6 +415,53 @@ int imex_write_tecplot(imex_lattice* h, const char* path, int n)
     cudaFreeAsync(d, h->stream);
     cudaStreamSynchronize(h->stream);
     return rc;
+}
+
+int imex_write_output(imex_lattice* h, const char* path, int n)
+{
+    int rc = ready(h, "imex_write_output");
+    if (rc) return rc;
+    const std::string name = path ? std::string(path) : "output" + std::to_string(n) + "0.dat";
+    const Geom& g = h->g;
+    // f(0), the rest population: streaming does not move it, so a pending
+    // streaming changes nothing here
+    std::vector<double> f0(h->ncells);
+    cudaError_t e = cudaSuccess;
+    if (h->precision == IMEX_F64) {
+        e = cudaMemcpyAsync(f0.data(), h->buf[h->cur], h->ncells * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
+    } else {
+        double* d = nullptr;
+        e = cudaMallocAsync(&d, (size_t)kQ * h->ncells * sizeof(double), h->stream);
+        if (e == cudaSuccess) e = launch_to_f64(h->precision, false, h->buf[h->cur], g, d, h->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(f0.data(), d, h->ncells * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
+        if (d) cudaFreeAsync(d, h->stream);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return cuda_fail(h, e, "imex_write_output: copy");
+    FILE* fp = std::fopen(name.c_str(), "wb");
+    if (!fp) return fail(h, IMEX_ERR_IO, "imex_write_output: cannot open " + name);
+    // src/lbm.cpp:606-627: a header, then one line "x y z f" per cell with x
+    // fastest, f fixed with 8 decimals (std::fixed, setprecision(8))
+    std::string out = "variables=x,y,z,f\n";
+    out += "zone I=" + std::to_string(g.nx) + ",J=" + std::to_string(g.ny) + ",K=" + std::to_string(g.nz) + "\n";
+    bool ok = true;
+    char line[96];
+    for (int k = 0; k < g.nz && ok; ++k)
+        for (int j = 0; j < g.ny && ok; ++j) {
+            for (int i = 0; i < g.nx; ++i) {
+                const int len = std::snprintf(line, sizeof line, "%d %d %d %.8f\n", i, j, k,
+                                              f0[((size_t)i * g.ny + j) * g.nz + k]);
+                out.append(line, (size_t)len);
+            }
+            if (out.size() > (1u << 22)) {
+                ok = std::fwrite(out.data(), 1, out.size(), fp) == out.size();
+                out.clear();
+            }
+        }
+    if (ok && !out.empty()) ok = std::fwrite(out.data(), 1, out.size(), fp) == out.size();
+    if (std::fclose(fp) != 0) ok = false;
+    return ok ? IMEX_OK : fail(h, IMEX_ERR_IO, "imex_write_output: write to " + name + " failed");
 }
 
 int imex_checkpoint_save(imex_lattice* h, const char* path)

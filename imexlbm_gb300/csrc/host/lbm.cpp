@@ -71,6 +71,7 @@ void LBM::fence() { check(imex_synchronize(h_)); }
 void LBM::ComputeMacroscopic(double* p, double* u, double* v, double* w) { check(imex_macroscopic(h_, p, u, v, w)); }
 
 void LBM::MPIoutput(int n) { check(imex_write_tecplot(h_, nullptr, n)); }
+void LBM::Output(int n) { check(imex_write_output(h_, nullptr, n)); }
 
 void LBM::profile_enable(bool on) { check(imex_profile_enable(h_, on ? 1 : 0)); }
 

@@ -73,6 +73,7 @@ struct LBM {
     void ComputeMacroscopic(double* p, double* u, double* v, double* w);
     void Conserved(double& mass, double& mom_x, double& mom_y, double& mom_z, double& ke);
     void MPIoutput(int n);  // lbm.cpp:307-598: writes output<n>.plt
+    void Output(int n);     // lbm.cpp:606-636: writes output<n>0.dat (f(0) as text)
     void fence();
     // per-phase device time of this lattice's kernels (imex_profile_*)
     void profile_enable(bool on);

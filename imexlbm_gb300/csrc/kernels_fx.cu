@@ -71,6 +71,34 @@ __global__ void __launch_bounds__(kStepBlock, 5) k_step_fx(const double* __restr
     if (!ok) fallback_cell(src, dst, g, i, j, k, cp, fallback);
 }
 
+// In-place collision of the fixed-point engine (a Collision() on a state
+// whose streaming is not pending: the first step of a run, or after the
+// distributions were set).  The same cell arithmetic as the fused kernels,
+// so every call order gives the same bits; a cell outside the exact range is
+// collided in native float64 from the inputs it still holds.
+template <bool OM_GE1>
+__global__ void __launch_bounds__(kStepBlock, 5) k_collide_fx(double* __restrict__ f, Geom g, FxConst c, CollideF64 cp,
+                                                           unsigned long long* __restrict__ fallback)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y, i = blockIdx.z;
+    if (k >= g.nz) return;
+    const size_t cell = ((size_t)i * g.ny + j) * g.nz + k;
+    double v[kQ], out[kQ];
+#pragma unroll
+    for (int a = 0; a < kQ; ++a) v[a] = f[(size_t)a * g.plane + cell];
+    bool ok = true;
+    fx::collide_cell<OM_GE1>(v, out, c, ok);
+    if (!ok) {
+        collide_f64(v, cp);
+#pragma unroll
+        for (int a = 0; a < kQ; ++a) out[a] = v[a];
+        atomicAdd(fallback, 1ull);
+    }
+#pragma unroll
+    for (int a = 0; a < kQ; ++a) f[(size_t)a * g.plane + cell] = out[a];
+}
+
 // The fused step inside a run of steps that keeps the state as X between
 // its launches (see launch_step_fx_run): IN_FX / OUT_FX read / write X on
 // the float64 grid instead of float64, which saves the 27 conversions each
@@ -185,10 +213,15 @@ cudaError_t launch_rows_fx(const double* src, double* dst, const Geom& g, const 
 cudaError_t launch_step_fx(int mode, const double* src, double* dst, const Geom& g, const FxParams& fx,
                            const CollideF64& cp, unsigned long long* fallback, cudaStream_t s)
 {
-    // The fixed-point kernel is the fused step; the one-off in-place
-    // collision (first step only) stays native.
-    if (mode != kModeFused) return launch_step_f64(mode, src, dst, g, cp, s);
+    // Streaming alone moves values and is engine-independent.
+    if (mode == kModeStream) return launch_step_f64(mode, src, dst, g, cp, s);
     const dim3 grid((g.nz + kStepBlock - 1) / kStepBlock, g.ny, g.nx);
+    if (mode == kModeCollide) {
+        if (src != dst) return cudaErrorInvalidValue;  // the collision is in place
+        if (fx.om_ge1) k_collide_fx<true><<<grid, kStepBlock, 0, s>>>(dst, g, fx.k, cp, fallback);
+        else k_collide_fx<false><<<grid, kStepBlock, 0, s>>>(dst, g, fx.k, cp, fallback);
+        return cudaGetLastError();
+    }
     if (fx.om_ge1)
         k_step_fx<true><<<grid, kStepBlock, 0, s>>>(src, dst, g, fx.k, cp, fallback);
     else

@@ -151,6 +151,13 @@ class LBM:
         self._check(self._L.imex_write_tecplot(self._h, name.encode(), int(n)))
         return name
 
+    def Output(self, n: int, path: str | None = None) -> str:
+        """Write the reference's ASCII dump of f(0), output<n>0.dat
+        (src/lbm.cpp:606-636), or ``path``; returns the file name."""
+        name = path if path is not None else f"output{int(n)}0.dat"
+        self._check(self._L.imex_write_output(self._h, name.encode(), int(n)))
+        return name
+
     def checkpoint_save(self, path: str) -> None:
         self._check(self._L.imex_checkpoint_save(self._h, str(path).encode()))
 

@@ -171,6 +171,14 @@ int imex_minmax_uvwp(imex_lattice *h, double out[8]);
  * Returns IMEX_ERR_IO if the file cannot be written.  Synchronises. */
 int imex_write_tecplot(imex_lattice *h, const char *path, int n);
 
+/* Write the ASCII dump of LBM::Output(n) (src/lbm.cpp:606-636) for this
+ * lattice: "variables=x,y,z,f", "zone I=nx,J=ny,K=nz", then one line
+ * "x y z f" per cell, x fastest, with the rest population f(0) in fixed
+ * notation with 8 decimals.  path NULL writes "output<n>0.dat" (the
+ * reference's name on rank 0).  Returns IMEX_ERR_IO if the file cannot be
+ * written.  Synchronises. */
+int imex_write_output(imex_lattice *h, const char *path, int n);
+
 /* Save the lattice's state - stored distributions in their storage
  * precision, the step count, whether a streaming is pending, the rounding
  * mode - to a file, and load it back into a lattice of the same size and

@@ -131,3 +131,28 @@ def test_checkpoint_errors(imex, tmp_path):
             other.step(1)                        # a failed load leaves the lattice uninitialised
         other.checkpoint_load(path)
         other.step(1)
+
+
+@pytest.mark.parametrize("name", PRECS)
+def test_ascii_output_equals_the_reference_format(imex, tmp_path, name):
+    """LBM::Output's ASCII dump of f(0) (src/lbm.cpp:606-636): the file equals
+    the reference's format (pinned against the reference's own file in
+    tests/test_reference_pin.py) applied to the lattice's own f, which a
+    pending streaming does not change."""
+    import sys
+    sys.path.insert(0, os.path.dirname(__file__))
+    from test_reference_pin import RUNS, ascii_dump
+    deck = imex.System(text=RUNS["files"]["deck"])
+    with imex.LBM(deck.sx, deck.sy, deck.sz, deck.tau, deck.rho0, deck.u0, precision=prec_id(imex, name)) as lat:
+        lat.Initialize()
+        lat.step(RUNS["files"]["steps"])
+        path = lat.Output(1, str(tmp_path / "o.dat"))
+        f = lat.get_f()
+    data = open(path, "rb").read()
+    assert data == ascii_dump(f)
+    assert data.decode().splitlines()[:2] == RUNS["files"]["ascii"]["head"][:2]
+    if name == "f64":
+        # within the reference's printed precision of the reference's own file
+        ref = [float(ln.split()[3]) for ln in RUNS["files"]["ascii"]["head"][2:]]
+        got = [float(ln.split()[3]) for ln in data.decode().splitlines()[2:6]]
+        assert np.allclose(got, ref, rtol=0, atol=1e-8)

@@ -108,3 +108,25 @@ def test_live_reference_run_matches_the_record(ref_exe):
         got = hashlib.sha256(open(os.path.join(d, "f.bin"), "rb").read()).hexdigest()
         assert got == rec["runs"]["2"]["f_sha256"]
         assert o.parse_cons(text)[-1] == tuple(rec["runs"]["2"]["dump_cons_last"])
+
+
+def ascii_dump(f: np.ndarray) -> bytes:
+    """LBM::Output's text (src/lbm.cpp:606-627) of f on one rank: a header,
+    then "x y z f(0)" per cell, x fastest, f in fixed notation, 8 decimals."""
+    _, nx, ny, nz = f.shape
+    lines = ["variables=x,y,z,f", f"zone I={nx},J={ny},K={nz}"]
+    f0 = f[0]
+    for k in range(nz):
+        for j in range(ny):
+            for i in range(nx):
+                lines.append(f"{i} {j} {k} {f0[i, j, k]:.8f}")
+    return ("\n".join(lines) + "\n").encode()
+
+
+def test_ascii_dump_format_is_the_references(oracle):
+    rec = RUNS["files"]
+    f, _ = oracle_run(oracle, rec["deck"], rec["steps"])
+    data = ascii_dump(f)
+    assert data.decode().splitlines()[:6] == rec["ascii"]["head"]
+    assert len(data) == rec["ascii"]["bytes"]
+    assert hashlib.sha256(data).hexdigest() == rec["ascii"]["sha256"]
