@@ -112,12 +112,15 @@ __device__ __forceinline__ void batch_cell(const BatchEntry& e, unsigned long lo
 }
 
 // CPT cells per thread, strided by blockDim within a chunk of CPT*blockDim.
-// PF = IMEX_F32: every member of the packed index is float32, and only that
-// path is compiled.  With one cell per thread it is held to 64 registers (4
-// CTAs of 256 threads per SM, no spills): at the compiler's 80 only 3 fit,
-// and the kernel, bound by global-load latency, ran at 28.1 GLUPS on the
-// 64-lattice float32 workload (28.7 now; the row kernel, 29.1, stays the
-// autotuner's choice there).
+// Every member starts on a chunk boundary of the packed index (upload_table
+// pads the index), so a chunk holds cells of one member only: the member is
+// looked up once per chunk, by a search all threads make on the same
+// shared-memory entries, and the cells are numbered within the member in
+// 32 bits.  (Searching per cell, 11 dependent shared-memory loads for 2048
+// members, held the float32 kernel at 28.1-28.7 GLUPS on the 64-lattice
+// workload.)  PF = IMEX_F32: every member of the packed index is float32,
+// and only that path is compiled, held to 64 registers with one cell per
+// thread (4 CTAs of 256 threads per SM).
 template <int CPT, int PF>
 __global__ void __launch_bounds__(256, (PF == IMEX_F32 && CPT == 1) ? 4 : 0)
     k_batch(const BatchHeader* __restrict__ hdr, const BatchEntry* __restrict__ tab, int s, CollideF32 base)
@@ -130,21 +133,23 @@ __global__ void __launch_bounds__(256, (PF == IMEX_F32 && CPT == 1) ? 4 : 0)
     __syncthreads();
     const unsigned long long chunk = (unsigned long long)blockDim.x * CPT;
     for (unsigned long long c0 = (unsigned long long)blockIdx.x * chunk; c0 < total; c0 += (unsigned long long)gridDim.x * chunk) {
+        int lo = 0, hi = count;  // largest lo with sbegin[lo] <= c0 (the same for every thread)
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (sbegin[mid] <= c0) lo = mid;
+            else hi = mid;
+        }
+        const BatchEntry& e = tab[lo];
+        if (s >= e.steps) continue;
+        const unsigned first = (unsigned)(c0 - sbegin[lo]) + threadIdx.x;
+        const unsigned cells = (unsigned)e.plane;
 #pragma unroll
         for (int c = 0; c < CPT; ++c) {
-            const unsigned long long q = c0 + (unsigned long long)c * blockDim.x + threadIdx.x;
-            if (q >= total) break;
-            int lo = 0, hi = count;  // largest lo with sbegin[lo] <= q
-            while (hi - lo > 1) {
-                const int mid = (lo + hi) >> 1;
-                if (sbegin[mid] <= q) lo = mid;
-                else hi = mid;
-            }
-            const BatchEntry& e = tab[lo];
-            if (s >= e.steps) continue;
-            if constexpr (PF == IMEX_F32) batch_cell<IMEX_F32>(e, q - sbegin[lo], s, base);
-            else if (e.prec == IMEX_F32) batch_cell<IMEX_F32>(e, q - sbegin[lo], s, base);
-            else batch_cell<IMEX_F16DEV>(e, q - sbegin[lo], s, base);
+            const unsigned local = first + (unsigned)c * blockDim.x;
+            if (local >= cells) break;
+            if constexpr (PF == IMEX_F32) batch_cell<IMEX_F32>(e, local, s, base);
+            else if (e.prec == IMEX_F32) batch_cell<IMEX_F32>(e, local, s, base);
+            else batch_cell<IMEX_F16DEV>(e, local, s, base);
         }
     }
 }
@@ -371,9 +376,12 @@ int rows_per_item(const imex_lattice* h, const RowShape& rs)
 }
 
 // Write the member tables for a tick where member m runs steps[m] fused
-// steps under row shape rs, and upload them (stream-ordered).
-int upload_table(imex_batch* b, const std::vector<int>& steps, const RowShape& rs)
+// steps under row shape rs and cell-kernel shape sh, and upload them
+// (stream-ordered).  In the cell kernel's packed index every member starts
+// on a boundary of sh's chunk (threads x cells per thread).
+int upload_table(imex_batch* b, const std::vector<int>& steps, const RowShape& rs, const BatchShape& sh)
 {
+    const unsigned long long chunk = (unsigned long long)(sh.threads > 0 ? sh.threads : 256) * (sh.cpt > 0 ? sh.cpt : 1);
     unsigned long long begin = 0;
     unsigned ibegin = 0;
     int n = 0, nr = 0, n16 = 0;
@@ -403,7 +411,7 @@ int upload_table(imex_batch* b, const std::vector<int>& steps, const RowShape& r
         } else {
             e.begin = begin;
             e.ibegin = 0;
-            begin += h->ncells;
+            begin += (h->ncells + chunk - 1) / chunk * chunk;
         }
     }
     b->h_hdr->total = begin;
@@ -486,7 +494,7 @@ std::vector<RowShape> row_candidates()
 int time_step(imex_batch* b, const BatchShape& sh, const RowShape& rs, float* ms)
 {
     std::vector<int> one(b->members.size(), 1);
-    int rc = upload_table(b, one, rs);
+    int rc = upload_table(b, one, rs, sh);
     if (rc) return rc;
     cudaEvent_t e0, e1;
     B_CUDA(b, cudaEventCreate(&e0), "cudaEventCreate");
@@ -541,7 +549,7 @@ int tune_batch(imex_batch* b, bool tune_cells, bool tune_rows)
     }
     if (tune_cells) {
         std::vector<int> one(b->members.size(), 1);
-        int rc = upload_table(b, one, b->rshape);
+        int rc = upload_table(b, one, b->rshape, b->shape);
         if (rc) return rc;
         if (b->n_cell > 0) {
             float best = 0.f;
@@ -723,7 +731,7 @@ int imex_batch_step(imex_batch* b, int nsteps)
         const int K = b->graph_steps > 0 ? b->graph_steps : 1;
         const int k = (int)std::min<int64_t>(most, K);
         for (size_t m = 0; m < left.size(); ++m) tick[m] = (int)std::min<int64_t>(left[m], k);
-        rc = upload_table(b, tick, b->rshape);
+        rc = upload_table(b, tick, b->rshape, b->shape);
         if (rc) return rc;
         if (b->graph_steps > 0 && k == b->graph_steps) {
             if (!graph_valid(b, k)) {

@@ -27,7 +27,7 @@
  * LayoutRight View with its 3 ghost layers stripped).
  *
  * Parity pin: bit for bit against the reference's own code.  The
- * reference's unmodified src/*.cpp, built against the single-process
+ * reference's unmodified src/ C++ files, built against the single-process
  * Kokkos / MPI stand-ins of oracle/refshim and run on 1 to 8 ranks,
  * produce fields whose SHA-256 this oracle reproduces exactly (32^3 and
  * 18x20x22 decks, 20-100 steps), `cons` lines it matches to the rounding of
