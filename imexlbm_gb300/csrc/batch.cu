@@ -34,7 +34,10 @@
 // only the members' spare buffers, so it changes no state.
 #include <algorithm>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "imexlbm.h"
@@ -121,11 +124,18 @@ __device__ __forceinline__ void batch_cell(const BatchEntry& e, unsigned long lo
 // workload.)  PF = IMEX_F32: every member of the packed index is float32,
 // and only that path is compiled, held to 64 registers with one cell per
 // thread (4 CTAs of 256 threads per SM).
-template <int CPT, int PF>
-__global__ void __launch_bounds__(256, (PF == IMEX_F32 && CPT == 1) ? 4 : 0)
+//
+// TPB / MINB: the launch bounds.  Threads 256 with 4 CTAs per SM (64
+// registers) for the float32-only kernel with one cell per thread, the
+// compiler's choice for the others; threads 128 with 9 CTAs per SM (56
+// registers, 36 warps per SM) for the lean float32 kernel, near the
+// occupancy of the one-lattice float32 kernel (48 registers, 128 threads,
+// 40 warps).
+template <int CPT, int PF, int TPB = 256, int MINB = (PF == IMEX_F32 && CPT == 1) ? 4 : 0>
+__global__ void __launch_bounds__(TPB, MINB)
     k_batch(const BatchHeader* __restrict__ hdr, const BatchEntry* __restrict__ tab, int s, CollideF32 base)
 {
-    __shared__ unsigned long long sbegin[kBatchMax + 1];
+    extern __shared__ unsigned long long sbegin[];  // count + 1 entries (the launch sizes it for the capacity)
     const int count = hdr->count;
     const unsigned long long total = hdr->total;
     for (int q = threadIdx.x; q < count; q += blockDim.x) sbegin[q] = tab[q].begin;
@@ -305,23 +315,54 @@ int kinds(const imex_batch* b)
 
 // One step (index s of the tick) of every member: the cell kernel over its
 // members, then the row kernel over its members.
+// Persistent grid of the cell kernel `fn` for shape sh: sh.ctas_per_sm CTAs
+// per SM, but no more than can be resident at once.  CTAs beyond the
+// resident ones would run their whole strided loop after the first wave,
+// reading rows whose neighbours the first wave has already evicted from L2.
+unsigned cell_grid(const imex_batch* b, const void* fn, const BatchShape& sh)
+{
+    static std::mutex lock;
+    static std::map<std::tuple<int, const void*, int>, int> cache;
+    const auto key = std::make_tuple(b->device * 4096 + b->capacity, fn, sh.threads);
+    int resident = 0;
+    {
+        std::lock_guard<std::mutex> guard(lock);
+        auto it = cache.find(key);
+        if (it != cache.end()) resident = it->second;
+    }
+    if (!resident) {
+        const size_t smem = sizeof(unsigned long long) * ((size_t)b->capacity + 1);
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, fn, sh.threads, smem) != cudaSuccess ||
+            resident < 1) {
+            cudaGetLastError();
+            resident = 1;
+        }
+        std::lock_guard<std::mutex> guard(lock);
+        cache[key] = resident;
+    }
+    return (unsigned)(b->sms * std::min(sh.ctas_per_sm, resident));
+}
+
+template <int C, int PF, int TPB = 256, int MINB = (PF == IMEX_F32 && C == 1) ? 4 : 0>
+cudaError_t launch_cells(imex_batch* b, const BatchShape& sh, int s, const CollideF32& base)
+{
+    auto* fn = k_batch<C, PF, TPB, MINB>;
+    const size_t smem = sizeof(unsigned long long) * ((size_t)b->capacity + 1);
+    fn<<<cell_grid(b, (const void*)fn, sh), sh.threads, smem, b->stream>>>(b->d_hdr, b->d_tab, s, base);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_step(imex_batch* b, const BatchShape& sh, const RowShape& rs, int s)
 {
     const CollideF32 base = base_constants();
     if (b->n_cell > 0) {
-        const dim3 grid((unsigned)(b->sms * sh.ctas_per_sm));
         const bool f32 = b->n_cell_f16 == 0;
-#define IMEX_BATCH_CELLS(C) \
-    (f32 ? k_batch<C, IMEX_F32><<<grid, sh.threads, 0, b->stream>>>(b->d_hdr, b->d_tab, s, base) \
-         : k_batch<C, 0><<<grid, sh.threads, 0, b->stream>>>(b->d_hdr, b->d_tab, s, base))
-        switch (sh.cpt) {
-        case 1: IMEX_BATCH_CELLS(1); break;
-        case 2: IMEX_BATCH_CELLS(2); break;
-        case 4: IMEX_BATCH_CELLS(4); break;
-        default: return cudaErrorInvalidValue;
-        }
-#undef IMEX_BATCH_CELLS
-        cudaError_t e = cudaGetLastError();
+        cudaError_t e;
+        if (f32 && sh.cpt == 1 && sh.threads == 128) e = launch_cells<1, IMEX_F32, 128, 9>(b, sh, s, base);
+        else if (sh.cpt == 1) e = f32 ? launch_cells<1, IMEX_F32>(b, sh, s, base) : launch_cells<1, 0>(b, sh, s, base);
+        else if (sh.cpt == 2) e = f32 ? launch_cells<2, IMEX_F32>(b, sh, s, base) : launch_cells<2, 0>(b, sh, s, base);
+        else if (sh.cpt == 4) e = f32 ? launch_cells<4, IMEX_F32>(b, sh, s, base) : launch_cells<4, 0>(b, sh, s, base);
+        else e = cudaErrorInvalidValue;
         if (e != cudaSuccess) return e;
     }
     if (b->n_row > 0) {
@@ -458,11 +499,11 @@ std::vector<BatchShape> candidates()
     std::vector<BatchShape> out;
     const int threads[2] = {128, 256};
     const int cpts[3] = {1, 2, 4};
-    const int ctas[3] = {2, 4, 8};
+    const int ctas[4] = {2, 4, 8, 9};
     for (int t : threads)
         for (int c : cpts)
             for (int k : ctas) {
-                if (t * k > 2048) continue;
+                if (t * k > 2048 || (k == 9 && (t != 128 || c != 1))) continue;  // 9: the lean kernel's residency
                 BatchShape s;
                 s.threads = t;
                 s.cpt = c;
