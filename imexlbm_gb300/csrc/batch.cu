@@ -80,17 +80,15 @@ struct RowsHeader {
     int count;       // its members
 };
 
+// Fused step of cell (i, j, k) of member e - its index `local` within the
+// member - at step s of the tick.
 template <int P>
-__device__ __forceinline__ void batch_cell(const BatchEntry& e, unsigned long long local, int s, const CollideF32& base)
+__device__ __forceinline__ void batch_cell_at(const BatchEntry& e, int i, int j, int k, unsigned local, int s,
+                                              const CollideF32& base)
 {
     using S = lowp::Storage<P>;
     using T = typename S::T;
     const int nz = e.nz, ny = e.ny, nx = e.nx;
-    const unsigned l32 = (unsigned)local;  // members hold fewer than 2^32 cells
-    const unsigned row = l32 / (unsigned)nz;
-    const int k = (int)(l32 - row * (unsigned)nz);
-    const int i = (int)(row / (unsigned)ny);
-    const int j = (int)(row - (unsigned)i * (unsigned)ny);
     Geom g;
     g.nx = nx;
     g.ny = ny;
@@ -112,6 +110,56 @@ __device__ __forceinline__ void batch_cell(const BatchEntry& e, unsigned long lo
 #pragma unroll
         for (int a = 0; a < kQ; ++a) dst[(size_t)a * e.plane + local] = S::store(h[a], a);
     }
+}
+
+template <int P>
+__device__ __forceinline__ void batch_cell(const BatchEntry& e, unsigned local, int s, const CollideF32& base)
+{
+    const unsigned row = local / (unsigned)e.nz;  // members hold fewer than 2^32 cells
+    const int k = (int)(local - row * (unsigned)e.nz);
+    const int i = (int)(row / (unsigned)e.ny);
+    const int j = (int)(row - (unsigned)i * (unsigned)e.ny);
+    batch_cell_at<P>(e, i, j, k, local, s, base);
+}
+
+// Cells per row segment of the one-CTA-per-segment cell kernel.
+constexpr int kUnitCells = kStepBlock;
+constexpr int kUnitGroup = 256;  // row segments per entry of the member lookup table
+
+// One CTA per row segment: the grid of the one-lattice kernel (k_step_lowp:
+// 128 threads per CTA, each CTA kUnitCells consecutive z-cells of one (x, y)
+// row), over every member of the cell kernel.  Segment u belongs to the
+// member whose first segment index `begin` is the largest not above u; the
+// member is found from group[u / kUnitGroup] (the member holding segment
+// u - u mod kUnitGroup) by stepping forward, the same for every thread of
+// the CTA, and the segment's (x, y, z block) is decoded once per CTA, so a
+// thread's cell costs what it costs in the one-lattice kernel.  The grid
+// covers the segments of the tick's members; a CUDA graph of these
+// launches is captured again when that count changes.  The float32-only
+// instantiation fits 48 registers (10 CTAs, 40 warps per SM, as the one-
+// lattice kernel); with the float16 path too it needs 64.
+template <int PF, int MINB = PF == IMEX_F32 ? 10 : 0>
+__global__ void __launch_bounds__(kUnitCells, MINB) k_batch_units(const BatchHeader* __restrict__ hdr,
+                                                            const BatchEntry* __restrict__ tab,
+                                                            const int* __restrict__ group, int s, CollideF32 base)
+{
+    const unsigned u = blockIdx.x;
+    const int count = hdr->count;
+    int m = group[u / kUnitGroup];
+    while (m + 1 < count && tab[m + 1].begin <= u) ++m;
+    const BatchEntry& e = tab[m];
+    if (s >= e.steps) return;
+    const unsigned zbs = ((unsigned)e.nz + kUnitCells - 1) / kUnitCells;
+    const unsigned seg = u - (unsigned)e.begin;
+    const unsigned row = seg / zbs;
+    const int k = (int)(seg - row * zbs) * kUnitCells + (int)threadIdx.x;
+    if (k >= e.nz) return;
+    const int i = (int)(row / (unsigned)e.ny);
+    const int j = (int)(row - (unsigned)i * (unsigned)e.ny);
+    const unsigned local = row * (unsigned)e.nz + (unsigned)k;
+    if constexpr (PF == IMEX_F32) batch_cell_at<IMEX_F32>(e, i, j, k, local, s, base);
+    else if (e.prec == IMEX_F32) batch_cell_at<IMEX_F32>(e, i, j, k, local, s, base);
+    else batch_cell_at<IMEX_F16DEV>(e, i, j, k, local, s, base);
 }
 
 // CPT cells per thread, strided by blockDim within a chunk of CPT*blockDim.
@@ -249,6 +297,9 @@ struct imex_batch {
     BatchEntry* d_rtab = nullptr;
     RowsHeader* h_rhdr = nullptr;
     BatchEntry* h_rtab = nullptr;
+    int* d_group = nullptr;     // one-CTA-per-segment cell kernel: member of every kUnitGroup-th segment
+    int* h_group = nullptr;
+    size_t group_cap = 0;
     unsigned* d_err = nullptr;  // set by the row kernel when a bounded wait runs out
     int capacity = 0;
     int device = 0;
@@ -261,6 +312,7 @@ struct imex_batch {
     cudaGraphExec_t graph = nullptr;
     int graph_k = 0;
     BatchShape graph_shape;
+    unsigned long long graph_units = 0;  // segments the captured cell-kernel launches cover
     RowShape graph_rshape;
     int graph_kinds = 0;  // bit 0: cell kernel, bit 1: row kernel, bit 2: cell kernel with float16 members
     int64_t launches = 0;
@@ -358,7 +410,16 @@ cudaError_t launch_step(imex_batch* b, const BatchShape& sh, const RowShape& rs,
     if (b->n_cell > 0) {
         const bool f32 = b->n_cell_f16 == 0;
         cudaError_t e;
-        if (f32 && sh.cpt == 1 && sh.threads == 128) e = launch_cells<1, IMEX_F32, 128, 9>(b, sh, s, base);
+        if (sh.cpt == 0) {  // one CTA per row segment
+            const unsigned long long units = b->h_hdr->total;
+            if (units == 0 || units > 0x7fffffffull) return cudaErrorInvalidValue;
+            if (f32)
+                k_batch_units<IMEX_F32><<<(unsigned)units, kUnitCells, 0, b->stream>>>(b->d_hdr, b->d_tab, b->d_group, s,
+                                                                                     base);
+            else
+                k_batch_units<0><<<(unsigned)units, kUnitCells, 0, b->stream>>>(b->d_hdr, b->d_tab, b->d_group, s, base);
+            e = cudaGetLastError();
+        } else if (f32 && sh.cpt == 1 && sh.threads == 128) e = launch_cells<1, IMEX_F32, 128, 9>(b, sh, s, base);
         else if (sh.cpt == 1) e = f32 ? launch_cells<1, IMEX_F32>(b, sh, s, base) : launch_cells<1, 0>(b, sh, s, base);
         else if (sh.cpt == 2) e = f32 ? launch_cells<2, IMEX_F32>(b, sh, s, base) : launch_cells<2, 0>(b, sh, s, base);
         else if (sh.cpt == 4) e = f32 ? launch_cells<4, IMEX_F32>(b, sh, s, base) : launch_cells<4, 0>(b, sh, s, base);
@@ -422,6 +483,7 @@ int rows_per_item(const imex_lattice* h, const RowShape& rs)
 // on a boundary of sh's chunk (threads x cells per thread).
 int upload_table(imex_batch* b, const std::vector<int>& steps, const RowShape& rs, const BatchShape& sh)
 {
+    const bool units = sh.cpt == 0;  // one CTA per row segment: the index counts segments
     const unsigned long long chunk = (unsigned long long)(sh.threads > 0 ? sh.threads : 256) * (sh.cpt > 0 ? sh.cpt : 1);
     unsigned long long begin = 0;
     unsigned ibegin = 0;
@@ -452,11 +514,37 @@ int upload_table(imex_batch* b, const std::vector<int>& steps, const RowShape& r
         } else {
             e.begin = begin;
             e.ibegin = 0;
-            begin += (h->ncells + chunk - 1) / chunk * chunk;
+            if (units)
+                begin += (unsigned long long)h->g.nx * h->g.ny * ((h->g.nz + kUnitCells - 1) / kUnitCells);
+            else
+                begin += (h->ncells + chunk - 1) / chunk * chunk;
         }
     }
     b->h_hdr->total = begin;
     b->h_hdr->count = n;
+    if (units && n > 0) {
+        if (begin > 0x7fffffffull) return bfail(b, IMEX_ERR_ARG, "imex_batch_step: too many row segments for one launch");
+        const size_t groups = (size_t)((begin + kUnitGroup - 1) / kUnitGroup);
+        if (groups > b->group_cap) {
+            if (b->d_group) cudaFreeAsync(b->d_group, b->stream);
+            if (b->h_group) cudaFreeHost(b->h_group);
+            b->d_group = nullptr;
+            b->h_group = nullptr;
+            b->group_cap = 0;
+            const size_t cap = groups * 2;
+            B_CUDA(b, cudaMallocAsync((void**)&b->d_group, cap * sizeof(int), b->stream), "cudaMallocAsync");
+            B_CUDA(b, cudaMallocHost((void**)&b->h_group, cap * sizeof(int)), "cudaMallocHost");
+            b->group_cap = cap;
+        }
+        int m = 0;
+        for (size_t q = 0; q < groups; ++q) {
+            const unsigned long long u = (unsigned long long)q * kUnitGroup;
+            while (m + 1 < n && b->h_tab[m + 1].begin <= u) ++m;
+            b->h_group[q] = m;
+        }
+        B_CUDA(b, cudaMemcpyAsync(b->d_group, b->h_group, groups * sizeof(int), cudaMemcpyHostToDevice, b->stream),
+               "cudaMemcpyAsync");
+    }
     b->h_rhdr->total = ibegin;
     b->h_rhdr->count = nr;
     b->n_cell = n;
@@ -497,6 +585,7 @@ int release_members(imex_batch* b)
 std::vector<BatchShape> candidates()
 {
     std::vector<BatchShape> out;
+    out.push_back(BatchShape{kUnitCells, 0, 0});  // one CTA per row segment
     const int threads[2] = {128, 256};
     const int cpts[3] = {1, 2, 4};
     const int ctas[4] = {2, 4, 8, 9};
@@ -630,6 +719,7 @@ int capture_graph(imex_batch* b, int K)
     b->graph_shape = b->shape;
     b->graph_rshape = b->rshape;
     b->graph_kinds = kinds(b);
+    b->graph_units = b->h_hdr->total;
     return IMEX_OK;
 }
 
@@ -639,7 +729,8 @@ bool graph_valid(const imex_batch* b, int K)
            b->graph_shape.cpt == b->shape.cpt && b->graph_shape.ctas_per_sm == b->shape.ctas_per_sm &&
            b->graph_rshape.stages == b->rshape.stages && b->graph_rshape.dir_kb == b->rshape.dir_kb &&
            b->graph_rshape.f32 == b->rshape.f32 &&
-           b->graph_rshape.ctas_per_sm == b->rshape.ctas_per_sm && b->graph_kinds == kinds(b);
+           b->graph_rshape.ctas_per_sm == b->rshape.ctas_per_sm && b->graph_kinds == kinds(b) &&
+           (b->shape.cpt != 0 || b->n_cell == 0 || b->graph_units == b->h_hdr->total);
 }
 
 }  // namespace
@@ -702,6 +793,8 @@ void imex_batch_destroy(imex_batch* b)
     if (b->h_rhdr) cudaFreeHost(b->h_rhdr);
     if (b->h_rtab) cudaFreeHost(b->h_rtab);
     if (b->d_err) cudaFree(b->d_err);
+    if (b->d_group) cudaFree(b->d_group);
+    if (b->h_group) cudaFreeHost(b->h_group);
     if (b->done) cudaEventDestroy(b->done);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
@@ -818,9 +911,16 @@ int imex_batch_set_launch(imex_batch* b, int threads, int cells_per_thread, int 
         b->shape = BatchShape{};
         return IMEX_OK;
     }
+    if (cells_per_thread == 0) {  // one CTA of 128 threads per row segment
+        if (threads != kUnitCells)
+            return bfail(b, IMEX_ERR_ARG, "imex_batch_set_launch: cells_per_thread 0 (one CTA per row segment) "
+                                          "takes 128 threads");
+        b->shape = BatchShape{kUnitCells, 0, 0};
+        return IMEX_OK;
+    }
     if ((threads != 128 && threads != 256) || (cells_per_thread != 1 && cells_per_thread != 2 && cells_per_thread != 4) ||
         ctas_per_sm < 1 || ctas_per_sm * threads > 2048)
-        return bfail(b, IMEX_ERR_ARG, "imex_batch_set_launch: threads 128|256, cells_per_thread 1|2|4, "
+        return bfail(b, IMEX_ERR_ARG, "imex_batch_set_launch: threads 128|256, cells_per_thread 0|1|2|4, "
                                       "ctas_per_sm*threads <= 2048");
     b->shape.threads = threads;
     b->shape.cpt = cells_per_thread;

@@ -319,8 +319,13 @@ int imex_batch_size(const imex_batch *b);
 int imex_batch_step(imex_batch *b, int nsteps);
 int imex_batch_synchronize(imex_batch *b);
 
-/* Pin the launch shape (threads 128|256, cells_per_thread 1|2|4,
- * ctas_per_sm * threads <= 2048), or threads = 0 to retune. */
+/* Pin the launch shape of the one-thread-per-cell kernel: a persistent
+ * grid (threads 128|256, cells_per_thread 1|2|4, ctas_per_sm * threads <=
+ * 2048; CTAs beyond those that can be resident are not launched), or
+ * cells_per_thread 0 with threads 128 - one CTA per 128-cell row segment of
+ * every member, the one-lattice kernel's grid over the whole batch (its
+ * CUDA graph is captured again when the members' segment count changes).
+ * threads = 0 retunes. */
 int imex_batch_set_launch(imex_batch *b, int threads, int cells_per_thread, int ctas_per_sm);
 int imex_batch_get_launch(imex_batch *b, int out[3]);
 

@@ -52,7 +52,7 @@ def test_batch_equals_alone(imex):
         lat.close()
 
 
-@pytest.mark.parametrize("shape", [(128, 1, 1), (256, 2, 4), (128, 4, 8), (256, 1, 2)])
+@pytest.mark.parametrize("shape", [(128, 1, 1), (256, 2, 4), (128, 4, 8), (256, 1, 2), (128, 1, 9), (128, 0, 0)])
 @pytest.mark.parametrize("graph", [0, 5])
 def test_batch_launch_shapes_and_graphs(imex, shape, graph):
     steps = 12
@@ -206,3 +206,29 @@ def test_batch_rejects_float64(imex):
         lat.Initialize()
         with pytest.raises(imex.ImexError):
             b.add(lat)
+
+
+def test_segment_kernel_graph_follows_the_members(imex):
+    """One CTA per row segment (cells_per_thread 0): the launch covers the
+    members' segments, so a member joining or leaving between ticks changes
+    the grid; the captured graph must follow, and every member still ends
+    where it ends alone."""
+    specs = SPECS[:4]
+    lats = [make(imex, s) for s in specs]
+    with imex.Batch(8) as b:
+        b.set_launch(128, 0, 0)
+        b.set_row_launch(-1)
+        b.set_graph(4)
+        for lat in lats[:2]:
+            b.add(lat)
+        b.step(8)                      # two members
+        for lat in lats[2:]:
+            b.add(lat)
+        b.step(8)                      # four: more segments
+        b.remove(lats[0])
+        b.step(8)                      # three
+        for lat, s in zip(lats, specs):
+            assert np.array_equal(lat.get_f(), alone(imex, s, lat.steps_done()))
+        assert b.get_launch() == (128, 0, 0)
+    for lat in lats:
+        lat.close()
