@@ -651,12 +651,15 @@ int time_step(imex_batch* b, const BatchShape& sh, const RowShape& rs, float* ms
 // members, and timed on that split.  Shapes pinned by imex_batch_set_launch
 // / imex_batch_set_row_launch are kept.  Each timing is one warm-up and
 // three steps of the whole batch, so the order matters for a large batch:
-// the row kernel usually takes every member, and the cell kernel's 15
-// shapes are then not timed at all.
+// float16-deviation members usually go to the row kernel and float32 ones
+// to the one-CTA-per-segment cell kernel, and the cell kernel's other
+// shapes are timed only on what is left to it.
 int tune_batch(imex_batch* b, bool tune_cells, bool tune_rows)
 {
     const RowShape off{-1, 0, 0, 1};
-    if (!b->shape.threads) b->shape = BatchShape{256, 1, 8};
+    // the row kernel's shapes are weighed against the cell kernel's usual
+    // best, one CTA per row segment
+    if (!b->shape.threads) b->shape = BatchShape{kUnitCells, 0, 0};
     if (tune_rows) {
         float best = 0.f;
         int rc = time_step(b, b->shape, off, &best);
