@@ -15,6 +15,7 @@
 // In the steady state Collision launches one fused kernel and Streaming
 // launches none.  Readers (Conserved, macroscopic, get_f) pull through S
 // when the state is kPending.
+#include <algorithm>
 #include <atomic>
 #include <cmath>
 #include <cstdio>
@@ -638,7 +639,15 @@ int step_fixed_run(imex_lattice* h, int n)
     int failed = 0;
     IMEX_CUDA(h, cudaMemcpyAsync(&failed, h->d_fail, sizeof failed, cudaMemcpyDeviceToHost, h->stream), "cudaMemcpy");
     IMEX_CUDA(h, cudaStreamSynchronize(h->stream), "fixed-point run");
-    if (failed > n) return IMEX_OK;
+    if (failed > n) {
+        h->fx_backoff = 0;
+        return IMEX_OK;
+    }
+    // A cell left the exact range: the next calls step one at a time (a
+    // run would likely fail again and be redone), for 1, 2, 4 .. 64 calls
+    // after successive failures, then a run is tried again.
+    h->fx_backoff = h->fx_backoff ? std::min(64, 2 * h->fx_backoff) : 1;
+    h->fx_skip = h->fx_backoff;
     // state after step failed - 1: the source buffer of step `failed`
     ++h->fx_reruns;
     h->cur = cur0 ^ ((failed - 1) & 1);
@@ -673,7 +682,13 @@ int imex_step(imex_lattice* h, int nsteps)
         }
         rc = ensure_tuned(h);
         if (rc) return rc;
-        if (h->rows.stages == 0 && !capturing(h)) return step_fixed_run(h, nsteps);
+        if (h->rows.stages == 0 && !capturing(h)) {
+            if (h->fx_skip > 0) {  // a recent run failed: step one at a time
+                --h->fx_skip;
+                return step_each(h, nsteps);
+            }
+            return step_fixed_run(h, nsteps);
+        }
     }
     return step_each(h, nsteps);
 }

@@ -49,6 +49,8 @@ struct imex_lattice {
     unsigned* d_err = nullptr;  // set by kernels whose bounded waits ran out
     int* d_fail = nullptr;      // first failing step of a fixed-point run (imex_step)
     int64_t fx_reruns = 0;      // fixed-point runs redone from a failing step
+    int fx_skip = 0;            // imex_step calls left that step one at a time after a failed run
+    int fx_backoff = 0;         // calls skipped after the last failure (doubles per failure, up to 64)
     RowConfig rows{};           // launch shape of the fused step (stages 0: one thread per cell)
     int shape_mode = -1;        // -1 autotune on first use, 0 one thread per cell, 1 row-staged
     bool shape_pinned = false;  // shape set by imex_set_launch rather than the autotuner

@@ -199,6 +199,14 @@ def test_fixed_point_run_redone_from_failing_step(imex, oracle):
         assert first is not None and first >= 3   # the run fails after its first launch
         assert a.fallback_cells() > 0
         assert np.array_equal(a.get_f(), b.get_f(), equal_nan=True)
+        # the failure is remembered: the next call steps one at a time (10
+        # launches) instead of a run that fails again and is redone
+        before = a.kernel_launches()
+        a.step(10)
+        assert a.kernel_launches() - before == 10
+        for _ in range(10):
+            b.step(1)
+        assert np.array_equal(a.get_f(), b.get_f(), equal_nan=True)
 
 
 def test_nonfinite_is_reported(imex):
