@@ -82,14 +82,15 @@ def load_peaks():
 
 
 def load_traffic(kernel: str):
-    """Per-cell DRAM bytes of `kernel` from the committed ncu summary, if any."""
+    """Per-cell DRAM bytes of `kernel` from the committed ncu summary and the
+    lattice size it was captured at, if any."""
     p = os.path.join(ROOT, "profiles", "dram_traffic.json")
     try:
         with open(p) as fp:
             d = json.load(fp)
-        return d[kernel]
+        return d[kernel], d.get("captured_at", {}).get(kernel, "?")
     except Exception:
-        return None
+        return None, None
 
 
 class ClockSampler:
@@ -433,10 +434,12 @@ def run_ours(a):
     bpc = BYTES_PER_CELL[a.precision]
     achieved = bpc * cells / (launch_ms * 1e-3) / 1e9
     kname = {"fixed": "step_fxs", "native": "step_f64", "float32": "step_lowp_" + a.precision}[eng_name]
-    tr = load_traffic(kname)
+    tr, tr_size = load_traffic(kname)
     roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
             "frac": round(achieved / hbm, 4), "peak_kind": peak_kind,
             "traffic": round(tr * cells, 0) if tr is not None else None,
+            "traffic_from": (f"ncu dram bytes per cell of a {tr_size} capture ({tr} B), times this launch's "
+                             f"{cells} cells (profiles/dram_traffic.json)") if tr is not None else None,
             "kernel": kname, "algorithmic_bytes_per_launch": bpc * cells}
 
     # end-to-end through the public API with host buffers
