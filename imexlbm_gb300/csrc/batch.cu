@@ -263,7 +263,7 @@ __global__ void __launch_bounds__(rowslp::kThreads, kMinBlocks)
         it.active = s < e.steps;
         return it;
     };
-    rowslp::run_items_split<kDirBytes, lowp::F2>(item_of, my, stages, base, smem, wc);
+    rowslp::run_items<kDirBytes, lowp::F2, true>(item_of, my, stages, base, smem, wc);
 }
 
 }  // namespace

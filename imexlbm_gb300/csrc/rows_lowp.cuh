@@ -42,8 +42,7 @@ namespace rowslp {
 
 constexpr int kThreads = 256;
 constexpr int kMaxStages = 16;
-constexpr int kBarBytes = 256;  // kMaxStages "full" mbarriers, or 8 "full" and 8 "empty" (run_items_split)
-constexpr int kMaxSplitStages = 8;
+constexpr int kBarBytes = 128;  // kMaxStages mbarriers
 
 // One work item.
 struct Item {
@@ -274,115 +273,6 @@ __device__ __forceinline__ void run_items(const ItemOf& item_of, int my, int sta
         }
         if (threadIdx.x == 0 && t + stages < my) arm(t + stages);  // stage s, next use
         __syncthreads();  // stage s may be refilled
-    }
-}
-
-// The batch kernel's item loop without a CTA-wide barrier per item.  Warp 0
-// alone arms the stages and issues the copies (lane a: direction a); every
-// warp releases a stage through its "empty" mbarrier (one arrival per warp)
-// when it has finished the item in it, and warp 0 refills the stage once all
-// eight have.  The other warps run ahead into the next staged item instead
-// of waiting for the slowest warp at the end of every item - with many short
-// items (small members) that wait dominated the run_items loop (barrier
-// stalls 2.6 per issue).  A wait that runs out sends the warp to the failure
-// path: it records the error; warp 0 first waits (bounded) for the latest
-// armed phase of every stage, so no copy is in flight when the CTA exits.
-// Every wait is bounded, and decisions after a wait are made warp-uniform
-// (__all_sync) so that no lane is left behind at a warp barrier.
-template <int kDirBytes, class Ar, class ItemOf>
-__device__ __forceinline__ void run_items_split(const ItemOf& item_of, int my, int stages, const CollideF32& base,
-                                                unsigned char* smem, const WaitCtl& wc)
-{
-    constexpr uint32_t kStage = (uint32_t)kQ * kDirBytes;
-    constexpr int nwarps = kThreads / 32;
-    uint64_t* full = reinterpret_cast<uint64_t*>(smem);
-    uint64_t* empty = full + kMaxSplitStages;
-    Item* slots = reinterpret_cast<Item*>(smem + kBarBytes);
-    unsigned char* ring = smem + kBarBytes + kSlotBytes;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int nslots = stages + 1;
-    int armed = 0;  // warp 0: items armed so far
-
-    auto arm = [&](int t) {  // warp 0, lane 0
-        const Item it = item_of(t);
-        slots[t % nslots] = it;
-        const uint32_t bytes = it.active ? (uint32_t)kQ * it.B * it.nz * elem_bytes(it.prec) : 0u;
-        bulk::mbar_arrive_expect_tx(&full[t % stages], bytes);
-    };
-    auto issue = [&](int t) {  // warp 0, lane a < 27, after arm(t) and a __syncwarp
-        const Item it = slots[t % nslots];
-        if (!it.active) return;
-        if (t == 0 && (int)blockIdx.x == wc.starve_cta) return;  // test hook: stage 0 never fills
-        const uint32_t es = elem_bytes(it.prec);
-        const uint32_t row_bytes = (uint32_t)it.nz * es;
-        const int a = lane, B = it.B, ny = it.ny;
-        int xs = it.x - ex(a, 0);
-        xs = xs < 0 ? xs + it.nx : xs >= it.nx ? xs - it.nx : xs;
-        const unsigned char* pl = it.src + ((size_t)a * it.plane + (size_t)xs * ny * it.nz) * es;
-        unsigned char* s = ring + (size_t)(t % stages) * kStage + (size_t)a * kDirBytes;
-        uint64_t* bar = &full[t % stages];
-        const int lo = it.y0 - ex(a, 1);
-        if (lo < 0) {
-            bulk::copy_g2s(s, pl + (size_t)(ny - 1) * row_bytes, row_bytes, bar);
-            if (B > 1) bulk::copy_g2s(s + row_bytes, pl, (uint32_t)(B - 1) * row_bytes, bar);
-        } else if (lo + B > ny) {
-            if (B > 1) bulk::copy_g2s(s, pl + (size_t)lo * row_bytes, (uint32_t)(B - 1) * row_bytes, bar);
-            bulk::copy_g2s(s + (size_t)(B - 1) * row_bytes, pl, row_bytes, bar);
-        } else {
-            bulk::copy_g2s(s, pl + (size_t)lo * row_bytes, (uint32_t)B * row_bytes, bar);
-        }
-    };
-    auto stage_in = [&](int t) {  // warp 0: arm and issue item t
-        if (lane == 0) arm(t);
-        __syncwarp();
-        if (lane < kQ) issue(t);
-        armed = t + 1;
-    };
-
-    if (threadIdx.x == 0) {
-        for (int q = 0; q < stages; ++q) {
-            bulk::mbar_init(&full[q], 1);
-            bulk::mbar_init(&empty[q], nwarps);
-        }
-        bulk::fence_mbar_init();
-    }
-    __syncthreads();
-    if (warp == 0)
-        for (int t = 0; t < stages && t < my; ++t) stage_in(t);
-
-    bool failed = false;
-    for (int t = 0; t < my && !failed; ++t) {
-        const int s = t % stages;
-        if (!__all_sync(0xffffffffu, bulk::mbar_wait(&full[s], (uint32_t)((t / stages) & 1), wc.cycles))) {
-            failed = true;
-            break;
-        }
-        const Item& it = slots[t % nslots];
-        if (it.active) {
-            if (it.prec == IMEX_F32) compute_item<IMEX_F32, kDirBytes, Ar>(ring + (size_t)s * kStage, it, base);
-            else compute_item<IMEX_F16DEV, kDirBytes, Ar>(ring + (size_t)s * kStage, it, base);
-        }
-        __syncwarp();
-        if (lane == 0) bulk::mbar_arrive(&empty[s]);
-        if (warp == 0 && t + stages < my) {
-            // every warp has left item t: stage s takes item t + stages
-            if (!__all_sync(0xffffffffu, bulk::mbar_wait(&empty[s], (uint32_t)((t / stages) & 1), wc.cycles))) {
-                failed = true;
-                break;
-            }
-            stage_in(t + stages);
-        }
-    }
-    if (!failed) return;
-    if (lane == 0) atomicOr(wc.err, 1u);
-    if (warp == 0 && lane == 0) {
-        // the latest armed phase of each stage: wait (bounded) for its copies
-        for (int q = 0; q < stages; ++q) {
-            int last = -1;
-            for (int t = armed - 1; t >= 0 && t >= armed - stages && last < 0; --t)
-                if (t % stages == q) last = t;
-            if (last >= 0) bulk::mbar_wait(&full[q], (uint32_t)((last / stages) & 1), wc.cycles);
-        }
     }
 }
 
