@@ -132,6 +132,150 @@ __global__ void __launch_bounds__(kStepBlock, 5)
     if (!ok) atomicMin(fail, j);
 }
 
+// ------------------------------------------------------ two steps a pass --
+// Two fused steps in one pass over HBM.  Phase A of a row (x, y) pulls
+// rows (x - ex, y - ey) of the source lattice and writes its collided
+// values (step j) into a ring of x-planes in device memory; phase B of row
+// (x, y) pulls from the ring and writes step j + 1 into the destination.
+// The ring - two pinned planes (x = 0 and 1, which the last rows of phase B
+// read) and R = kTwoRing recycled ones - is small enough to stay in L2, so
+// per two cell updates HBM sees one read of the source and one write of the
+// destination instead of two of each.
+//
+// Order.  CTAs take tickets from a counter; a ticket names one row of one
+// phase: A rows in x-major order, B rows (planes 1 .. nx-1, then plane 0;
+// in a plane rows 1 .. ny-1, then row 0, whose pull wraps to row ny-1)
+// interleaved 2 ny + 3 tickets behind, so that every row a ticket waits for
+// has a smaller ticket (checked on the host for nx 8..512, ny 4..256):
+// B(x, y) needs A of rows (x +- 1, y +- 1); A(x, y) of a recycled ring slot
+// needs B of the rows of planes x - R - 1 .. x - R + 1 that read it.  A waiting thread reads a
+// per-row flag (the launch's epoch once the row is written) with acquire
+// semantics; a CTA publishes a row by a __syncthreads, a fence and a release
+// store of its flag.  The rows waited for are held by CTAs that took their
+// tickets earlier and are running, so every wait ends; each wait is bounded
+// all the same, and one that runs out sets the error flag and ends the CTA.
+// Ring values are read with ld.global.cg (L2, never a stale L1 line of a
+// recycled slot).  The cell arithmetic is k_step_fxs's, fixed point in and
+// out, so the results are those of two single launches, bit for bit.
+constexpr int kTwoRing = 4;
+
+__device__ __forceinline__ int ld_acquire(const int* p)
+{
+    int v;
+    asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_release(int* p, int v)
+{
+    asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Ring slot of x-plane x.
+__device__ __forceinline__ int two_slot(int x) { return x < 2 ? x : 2 + (x - 2) % kTwoRing; }
+
+template <bool OM_GE1>
+__global__ void __launch_bounds__(kStepBlock, 5)
+    k_two_fxs(const unsigned long long* __restrict__ src, unsigned long long* __restrict__ dst, Geom g, FxConst c,
+              TwoStepCtl ts, int j, int* __restrict__ fail)
+{
+    __shared__ int s_ticket, s_abort;
+    if (*fail < j) return;  // an earlier step of the run failed
+    const int nx = g.nx, ny = g.ny, nz = g.nz;
+    const int N = nx * ny, L = 2 * ny + 3, T = 2 * N;
+    const size_t mplane = (size_t)(kTwoRing + 2) * ny * nz;  // ring values per direction
+    unsigned long long* mid = ts.mid;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            s_ticket = (int)atomicAdd(ts.counter, 1u);
+            s_abort = 0;
+        }
+        __syncthreads();
+        const int t = s_ticket;
+        if (t >= T) return;
+        // the ticket's phase and row
+        bool isA;
+        int r;
+        if (t < L) { isA = true; r = t; }
+        else if (t < T - L) { const int u = t - L; isA = u & 1; r = isA ? L + (u >> 1) : (u >> 1); }
+        else { isA = false; r = t - N; }
+        int x, y;
+        if (isA) {
+            x = r / ny;
+            y = r - x * ny;
+        } else {  // planes 1 .. nx-1 then 0; in a plane rows 1 .. ny-1 then 0
+            const int p = r / ny, q = r - p * ny;
+            x = p < nx - 1 ? p + 1 : 0;
+            y = q < ny - 1 ? q + 1 : 0;
+        }
+        // wait for the rows this one reads (B) or whose ring slot it reuses (A)
+        if (threadIdx.x == 0) {
+            const int* flags = isA ? ts.flag_b : ts.flag_a;
+            const int x0 = isA ? x - kTwoRing - 1 : x - 1;
+            const bool needed = !isA || x >= kTwoRing + 2;
+            bool ok = true;
+            for (int dx = 0; dx < 3 && needed && ok; ++dx)
+                for (int dy = -1; dy <= 1 && ok; ++dy) {
+                    int xx = x0 + dx;
+                    xx = xx < 0 ? xx + nx : xx >= nx ? xx - nx : xx;
+                    int yy = y + dy;
+                    yy = yy < 0 ? yy + ny : yy >= ny ? yy - ny : yy;
+                    const int* f = flags + (size_t)xx * ny + yy;
+                    if (ld_acquire(f) == ts.epoch) continue;
+                    const long long t0 = clock64();
+                    while (ld_acquire(f) != ts.epoch)
+                        if (clock64() - t0 > ts.cycles) {
+                            ok = false;
+                            break;
+                        }
+                }
+            if (!ok) {
+                atomicOr(ts.err, 1u);
+                s_abort = 1;
+            }
+        }
+        __syncthreads();
+        if (s_abort) return;
+        const int xm = x == 0 ? nx - 1 : x - 1, xp = x == nx - 1 ? 0 : x + 1;
+        const int ym = y == 0 ? ny - 1 : y - 1, yp = y == ny - 1 ? 0 : y + 1;
+        for (int k = threadIdx.x; k < nz; k += blockDim.x) {
+            const int km = k == 0 ? nz - 1 : k - 1, kp = k == nz - 1 ? 0 : k + 1;
+            const int xs[3] = {xp, x, xm}, ys[3] = {yp, y, ym}, zs[3] = {kp, k, km};  // by e + 1: source x - e
+            uint64_t in[kQ], out[kQ];
+            if (isA) {
+#pragma unroll
+                for (int a = 0; a < kQ; ++a)
+                    in[a] = __ldg(src + (size_t)a * g.plane +
+                                  ((size_t)xs[ex(a, 0) + 1] * ny + ys[ex(a, 1) + 1]) * nz +
+                                  zs[ex(a, 2) + 1]);
+            } else {
+#pragma unroll
+                for (int a = 0; a < kQ; ++a)
+                    in[a] = __ldcg(mid + (size_t)a * mplane +
+                                   ((size_t)two_slot(xs[ex(a, 0) + 1]) * ny + ys[ex(a, 1) + 1]) * nz +
+                                   zs[ex(a, 2) + 1]);
+            }
+            bool ok = true;
+            fx::collide_cell_io<OM_GE1, true, true>(in, out, c, ok);
+            if (isA) {
+                const size_t cell = ((size_t)two_slot(x) * ny + y) * nz + k;
+#pragma unroll
+                for (int a = 0; a < kQ; ++a) __stcg(mid + (size_t)a * mplane + cell, out[a]);
+            } else {
+                const size_t cell = ((size_t)x * ny + y) * nz + k;
+#pragma unroll
+                for (int a = 0; a < kQ; ++a) dst[(size_t)a * g.plane + cell] = out[a];
+            }
+            if (!ok) atomicMin(fail, j);
+        }
+        __syncthreads();  // every value of the row is stored
+        if (threadIdx.x == 0) {
+            __threadfence();
+            st_release((isA ? ts.flag_a : ts.flag_b) + (size_t)x * ny + y, ts.epoch);
+        }
+    }
+}
+
 // X (on the float64 grid) -> float64, in place.
 __global__ void k_fx_to_f64(unsigned long long* __restrict__ buf, size_t n)
 {
@@ -237,6 +381,25 @@ cudaError_t launch_step_fx_run(const double* src, double* dst, const Geom& g, co
     auto* out = reinterpret_cast<unsigned long long*>(dst);
     return fx.om_ge1 ? launch_fxs<true>(in, out, g, fx.k, j, n, fail, s)
                      : launch_fxs<false>(in, out, g, fx.k, j, n, fail, s);
+}
+
+bool two_step_eligible(const Geom& g) { return g.nx >= kTwoRing + 4 && g.ny >= 4 && (size_t)g.nx * g.ny < (1u << 30); }
+
+size_t two_step_ring_values(const Geom& g) { return (size_t)kQ * (kTwoRing + 2) * g.ny * g.nz; }
+
+cudaError_t launch_two_step_fx(const double* src, double* dst, const Geom& g, const FxParams& fx, const TwoStepCtl& ts,
+                               int j, int* fail, cudaStream_t s)
+{
+    if (!two_step_eligible(g)) return cudaErrorInvalidValue;
+    cudaError_t e = cudaMemsetAsync(ts.counter, 0, sizeof(unsigned), s);
+    if (e != cudaSuccess) return e;
+    // persistent: the CTAs that can be resident (5 per SM by the launch bounds)
+    const unsigned grid = (unsigned)(current_sm_count() * 5);
+    const auto* in = reinterpret_cast<const unsigned long long*>(src);
+    auto* out = reinterpret_cast<unsigned long long*>(dst);
+    if (fx.om_ge1) k_two_fxs<true><<<grid, kStepBlock, 0, s>>>(in, out, g, fx.k, ts, j, fail);
+    else k_two_fxs<false><<<grid, kStepBlock, 0, s>>>(in, out, g, fx.k, ts, j, fail);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_fx_to_f64(double* buf, size_t n, cudaStream_t s)

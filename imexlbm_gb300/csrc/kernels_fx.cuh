@@ -18,6 +18,26 @@ cudaError_t launch_step_fx(int mode, const double* src, double* dst, const Geom&
 // buffer, as X unless *fail is 1).
 cudaError_t launch_step_fx_run(const double* src, double* dst, const Geom& g, const FxParams& fx, int j, int n,
                                int* fail, cudaStream_t s);
+// Two fused steps in one pass (k_two_fxs): state as X in and out.  The
+// control block names the row-ticket counter, the per-row flags of both
+// phases (epoch-stamped, never reset), the L2-resident ring of
+// two_step_ring_values(g) values, the launch's epoch (> every earlier one),
+// the bounded wait in SM clocks and the error flag a wait that runs out sets.
+struct TwoStepCtl {
+    unsigned* counter;
+    int* flag_a;
+    int* flag_b;
+    unsigned long long* mid;
+    int epoch;
+    long long cycles;
+    unsigned* err;
+};
+bool two_step_eligible(const Geom& g);
+size_t two_step_ring_values(const Geom& g);
+// Steps j and j + 1 of a fixed-point run (X in, X out; *fail as for
+// launch_step_fx_run, set to j if either step leaves the exact range).
+cudaError_t launch_two_step_fx(const double* src, double* dst, const Geom& g, const FxParams& fx, const TwoStepCtl& ts,
+                               int j, int* fail, cudaStream_t s);
 // X on the float64 grid -> float64, in place, n values.
 cudaError_t launch_fx_to_f64(double* buf, size_t n, cudaStream_t s);
 struct RowConfig;

@@ -22,6 +22,7 @@
 #include <cstring>
 #include <map>
 #include <mutex>
+#include <utility>
 #include <new>
 #include <string>
 #include <tuple>
@@ -278,6 +279,70 @@ int time_fixed_run(imex_lattice* h, int reps, float* ms)
     return IMEX_OK;
 }
 
+int check_kernel_error(imex_lattice* h);
+
+// Resources of the two-steps-per-launch kernel (allocated once per handle):
+// the ticket counter, 2 nx ny row flags (zero: no epoch yet) and the ring.
+int ensure_two_step(imex_lattice* h)
+{
+    if (h->two_mem) return IMEX_OK;
+    const size_t rows = (size_t)h->g.nx * h->g.ny;
+    const size_t ring = two_step_ring_values(h->g) * sizeof(unsigned long long);
+    const size_t head = (16 + 2 * rows * sizeof(int) + 255) & ~(size_t)255;
+    unsigned char* m = nullptr;
+    IMEX_CUDA(h, cudaMallocAsync((void**)&m, head + ring, h->stream), "cudaMallocAsync");
+    IMEX_CUDA(h, cudaMemsetAsync(m, 0, head, h->stream), "cudaMemset");
+    h->two_mem = m;
+    h->two.counter = reinterpret_cast<unsigned*>(m);
+    h->two.flag_a = reinterpret_cast<int*>(m + 16);
+    h->two.flag_b = h->two.flag_a + rows;
+    h->two.mid = reinterpret_cast<unsigned long long*>(m + head);
+    h->two.err = h->d_err;
+    h->bytes += head + ring;
+    return IMEX_OK;
+}
+
+// Steps j, j + 1 of a run in one launch of the two-step kernel.
+cudaError_t launch_two(imex_lattice* h, const double* src, double* dst, int j)
+{
+    h->two.epoch = ++h->two_epoch;
+    h->two.cycles = make_wait_ctl(h->d_err).cycles;
+    return launch_two_step_fx(src, dst, h->g, h->fx, h->two, j, h->d_fail, h->stream);
+}
+
+// The two-steps-per-launch form of the run (stages 1): milliseconds per
+// step of `reps` launches from X in the spare buffer into a temporary third
+// buffer, as time_fixed_run times the one-step form.
+int time_two_run(imex_lattice* h, int reps, float* ms)
+{
+    int rc = ensure_two_step(h);
+    if (rc) return rc;
+    const size_t bytes = (size_t)kQ * h->ncells * sizeof(double);
+    double* tmp = nullptr;
+    IMEX_CUDA(h, cudaMallocAsync(&tmp, bytes, h->stream), "cudaMallocAsync");
+    double* x = dbuf(h, 1 - h->cur);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    const int n = 2 * reps + 2;
+    cudaError_t e = cudaMemsetAsync(h->d_fail, 0x7f, sizeof(int), h->stream);
+    if (e == cudaSuccess) e = launch_step_fx_run(dbuf(h, h->cur), x, h->g, h->fx, 1, n, h->d_fail, h->stream);
+    if (e == cudaSuccess) e = cudaEventCreate(&e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&e1);
+    if (e == cudaSuccess) e = cudaEventRecord(e0, h->stream);
+    for (int r = 0; r < reps && e == cudaSuccess; ++r) e = launch_two(h, x, tmp, 2 + 2 * r);
+    if (e == cudaSuccess) e = cudaEventRecord(e1, h->stream);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    float t = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&t, e0, e1);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaError_t e2 = cudaFreeAsync(tmp, h->stream);
+    if (e == cudaSuccess) e = e2;
+    if (e != cudaSuccess) return cuda_fail(h, e, "autotune");
+    h->launches += reps + 1;
+    *ms = t / (2 * reps);
+    return check_kernel_error(h);
+}
+
 // Time every candidate in interleaved rounds (so that a drift of the clock
 // or of the memory system during tuning does not favour one candidate) and
 // keep each candidate's fastest round; the fastest candidate wins.
@@ -285,6 +350,11 @@ int tune(imex_lattice* h)
 {
     std::vector<RowConfig> cands = row_candidates(h);
     RowConfig best{};  // classic
+    if (use_fixed(h) && two_step_eligible(h->g)) {
+        RowConfig two{};
+        two.stages = 1;  // one thread per cell, two steps per launch
+        cands.insert(cands.begin(), two);
+    }
     if (!cands.empty()) {
         cands.insert(cands.begin(), RowConfig{});
         std::vector<float> fastest(cands.size(), 0.f);
@@ -292,7 +362,9 @@ int tune(imex_lattice* h)
             for (size_t c = 0; c < cands.size(); ++c) {
                 float ms = 0.f;
                 const int reps = round == 0 ? 1 : 4;  // round 0 warms up
-                int rc = c == 0 && use_fixed(h) ? time_fixed_run(h, reps, &ms) : time_shape(h, cands[c], reps, &ms);
+                int rc = cands[c].stages == 1 ? time_two_run(h, reps, &ms)
+                         : c == 0 && use_fixed(h) ? time_fixed_run(h, reps, &ms)
+                                                  : time_shape(h, cands[c], reps, &ms);
                 if (rc) return rc;
                 if (round == 1 || ms < fastest[c]) fastest[c] = ms;
             }
@@ -318,7 +390,7 @@ int ensure_tuned(imex_lattice* h)
         auto it = g_tune_cache.find(tune_key(h));
         if (it != g_tune_cache.end()) {
             h->rows = it->second;
-            h->shape_mode = h->rows.stages > 0 ? 1 : 0;
+            h->shape_mode = h->rows.stages > 1 ? 1 : 0;
             return IMEX_OK;
         }
     }
@@ -327,12 +399,12 @@ int ensure_tuned(imex_lattice* h)
     if (cs != cudaStreamCaptureStatusNone) {
         std::vector<RowConfig> c = row_candidates(h);
         h->rows = c.empty() ? RowConfig{} : c.front();
-        h->shape_mode = h->rows.stages > 0 ? 1 : 0;
+        h->shape_mode = h->rows.stages > 1 ? 1 : 0;
         return IMEX_OK;
     }
     int rc = tune(h);
     if (rc) return rc;
-    h->shape_mode = h->rows.stages > 0 ? 1 : 0;
+    h->shape_mode = h->rows.stages > 1 ? 1 : 0;
     return IMEX_OK;
 }
 
@@ -349,7 +421,7 @@ int launch_mode(imex_lattice* h, int mode)
     }
     h->cf32.seed = (uint32_t)h->steps;  // stochastic rounding: a new stream of bits every step
     PhaseScope timed(h->prof, mode == kModeStream ? IMEX_PHASE_STREAM : IMEX_PHASE_COLLISION, h->stream);
-    if (mode == kModeFused && h->rows.stages > 0)
+    if (mode == kModeFused && h->rows.stages > 1)
         e = launch_fused_rows(h, src, dst, h->rows);
     else if (is_lowp(h))
         e = launch_step_lowp(h->precision, mode, src, dst, h->g, h->cf32, h->stream);
@@ -525,6 +597,7 @@ void imex_destroy(imex_lattice* h)
         for (void* p : h->buf)
             if (p) cudaFreeAsync(p, h->own_stream);
         if (h->scratch) cudaFreeAsync(h->scratch, h->own_stream);
+        if (h->two_mem) cudaFreeAsync(h->two_mem, h->own_stream);
         cudaStreamDestroy(h->own_stream);
     }
     delete h;
@@ -625,20 +698,37 @@ int step_each(imex_lattice* h, int nsteps)
 // that flag), so it is not used while the stream is being captured.
 int step_fixed_run(imex_lattice* h, int n)
 {
-    const int cur0 = h->cur;
     const int64_t steps0 = h->steps;
+    // the launches of the run: first step and the buffer each reads
+    std::vector<std::pair<int, int>> runs;
+    const bool two = h->rows.stages == 1;  // two steps per launch where it can
+    if (two) {
+        int rc = ensure_two_step(h);
+        if (rc) return rc;
+    }
     IMEX_CUDA(h, cudaMemsetAsync(h->d_fail, 0x7f, sizeof(int), h->stream), "cudaMemset");
-    for (int j = 1; j <= n; ++j) {
+    for (int j = 1; j <= n;) {
         PhaseScope timed(h->prof, IMEX_PHASE_COLLISION, h->stream);
-        IMEX_CUDA(h, launch_step_fx_run(dbuf(h, h->cur), dbuf(h, 1 - h->cur), h->g, h->fx, j, n, h->d_fail, h->stream),
-                  "step kernel launch");
+        runs.emplace_back(j, h->cur);
+        // a pair holds fixed point in and out: not the run's first or last step
+        const bool pair = two && j > 1 && j + 1 < n;
+        cudaError_t e = pair ? launch_two(h, dbuf(h, h->cur), dbuf(h, 1 - h->cur), j)
+                             : launch_step_fx_run(dbuf(h, h->cur), dbuf(h, 1 - h->cur), h->g, h->fx, j, n, h->d_fail,
+                                                  h->stream);
+        IMEX_CUDA(h, e, "step kernel launch");
         ++h->launches;
         h->cur = 1 - h->cur;
-        ++h->steps;
+        const int k = pair ? 2 : 1;
+        h->steps += k;
+        j += k;
     }
     int failed = 0;
     IMEX_CUDA(h, cudaMemcpyAsync(&failed, h->d_fail, sizeof failed, cudaMemcpyDeviceToHost, h->stream), "cudaMemcpy");
     IMEX_CUDA(h, cudaStreamSynchronize(h->stream), "fixed-point run");
+    if (two) {
+        int rc = check_kernel_error(h);  // a bounded wait of the two-step kernel ran out
+        if (rc) return rc;
+    }
     if (failed > n) {
         h->fx_backoff = 0;
         return IMEX_OK;
@@ -648,9 +738,11 @@ int step_fixed_run(imex_lattice* h, int n)
     // after successive failures, then a run is tried again.
     h->fx_backoff = h->fx_backoff ? std::min(64, 2 * h->fx_backoff) : 1;
     h->fx_skip = h->fx_backoff;
-    // state after step failed - 1: the source buffer of step `failed`
+    // state after step failed - 1: the source buffer of the launch that
+    // began with step `failed` (a two-step launch records its first step)
     ++h->fx_reruns;
-    h->cur = cur0 ^ ((failed - 1) & 1);
+    for (const auto& r : runs)
+        if (r.first == failed) h->cur = r.second;
     h->steps = steps0 + failed - 1;
     if (failed > 1) IMEX_CUDA(h, launch_fx_to_f64(dbuf(h, h->cur), (size_t)kQ * h->ncells, h->stream), "conversion");
     return step_each(h, n - failed + 1);
@@ -682,7 +774,7 @@ int imex_step(imex_lattice* h, int nsteps)
         }
         rc = ensure_tuned(h);
         if (rc) return rc;
-        if (h->rows.stages == 0 && !capturing(h)) {
+        if (h->rows.stages <= 1 && !capturing(h)) {  // one thread per cell (1: two steps per launch)
             if (h->fx_skip > 0) {  // a recent run failed: step one at a time
                 --h->fx_skip;
                 return step_each(h, nsteps);
@@ -942,8 +1034,12 @@ int imex_set_launch(imex_lattice* h, int stages, int rows_per_stage, int ctas_pe
         h->shape_pinned = false;
         return IMEX_OK;
     }
-    if (stages == 0) {
+    if (stages == 0 || stages == 1) {
+        if (stages == 1 && !(use_fixed(h) && two_step_eligible(h->g)))
+            return fail(h, IMEX_ERR_ARG, "imex_set_launch: two steps per launch (stages 1) needs the float64 fixed-point "
+                                         "engine and nx >= 8, ny >= 4");
         h->rows = RowConfig{};
+        h->rows.stages = stages;
         h->shape_mode = 0;
         h->shape_pinned = true;
         return IMEX_OK;
@@ -981,9 +1077,9 @@ int imex_get_launch(imex_lattice* h, int out[4])
     int rc = ensure_tuned(h);
     if (rc) return rc;
     out[0] = h->rows.stages;
-    out[1] = h->rows.stages ? h->rows.rows : 0;
+    out[1] = h->rows.stages > 1 ? h->rows.rows : 0;
     out[2] = h->rows.ctas_per_sm;
-    out[3] = h->rows.stages ? h->rows.threads : kStepBlock;  // one thread per cell: blocks of kStepBlock
+    out[3] = h->rows.stages > 1 ? h->rows.threads : kStepBlock;  // one thread per cell: blocks of kStepBlock
     return IMEX_OK;
 }
 

@@ -50,6 +50,11 @@ struct imex_lattice {
     int* d_fail = nullptr;      // first failing step of a fixed-point run (imex_step)
     int64_t fx_reruns = 0;      // fixed-point runs redone from a failing step
     int fx_skip = 0;            // imex_step calls left that step one at a time after a failed run
+    // two fused steps per launch (launch_two_step_fx): ticket counter, row
+    // flags of both phases and the L2-resident ring, allocated on first use
+    unsigned char* two_mem = nullptr;
+    imex::TwoStepCtl two{};
+    int two_epoch = 0;
     int fx_backoff = 0;         // calls skipped after the last failure (doubles per failure, up to 64)
     RowConfig rows{};           // launch shape of the fused step (stages 0: one thread per cell)
     int shape_mode = -1;        // -1 autotune on first use, 0 one thread per cell, 1 row-staged

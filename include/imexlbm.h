@@ -229,7 +229,12 @@ int imex_set_f_device(imex_lattice *h, const double *dev, size_t n);
 int imex_conserved_noalloc(const double *f_dev, int nx, int ny, int nz, double *out_dev, void *stream);
 
 /* Launch shape of the fused step.  stages = 0: one thread per cell pulling
- * straight from global memory.  stages >= 2: the row-staged kernel - each
+ * straight from global memory.  stages = 1 (float64 fixed-point engine, nx
+ * >= 8, ny >= 4): the same, with imex_step's runs taking two steps per
+ * launch - the first step's values go to a ring of x-planes small enough to
+ * stay in L2 and the second step reads them there, rows ordered across the
+ * GPU by tickets and per-row flags (bounded waits); the numbers are the
+ * one-step form's, bit for bit.  stages >= 2: the row-staged kernel - each
  * CTA keeps a ring of `stages` work items in shared memory, an item being
  * rows_per_stage consecutive y-rows (dividing ny for float64; for reduced
  * precision the last item of a plane takes the rows left) whose 27 source row runs
