@@ -138,27 +138,31 @@ __global__ void __launch_bounds__(kStepBlock, 5)
 // values (step j) into a ring of x-planes in device memory; phase B of row
 // (x, y) pulls from the ring and writes step j + 1 into the destination.
 // The ring - two pinned planes (x = 0 and 1, which the last rows of phase B
-// read) and R = kTwoRing recycled ones - is small enough to stay in L2, so
-// per two cell updates HBM sees one read of the source and one write of the
-// destination instead of two of each.
+// read) and R recycled ones - is meant to stay in L2, so per two cell
+// updates HBM sees one read of the source and one write of the destination
+// instead of two of each.
 //
 // Order.  CTAs take tickets from a counter; a ticket names one row of one
 // phase: A rows in x-major order, B rows (planes 1 .. nx-1, then plane 0;
 // in a plane rows 1 .. ny-1, then row 0, whose pull wraps to row ny-1)
-// interleaved 2 ny + 3 tickets behind, so that every row a ticket waits for
-// has a smaller ticket (checked on the host for nx 8..512, ny 4..256):
-// B(x, y) needs A of rows (x +- 1, y +- 1); A(x, y) of a recycled ring slot
-// needs B of the rows of planes x - R - 1 .. x - R + 1 that read it.  A waiting thread reads a
-// per-row flag (the launch's epoch once the row is written) with acquire
-// semantics; a CTA publishes a row by a __syncthreads, a fence and a release
-// store of its flag.  The rows waited for are held by CTAs that took their
-// tickets earlier and are running, so every wait ends; each wait is bounded
-// all the same, and one that runs out sets the error flag and ends the CTA.
-// Ring values are read with ld.global.cg (L2, never a stale L1 line of a
-// recycled slot).  The cell arithmetic is k_step_fxs's, fixed point in and
-// out, so the results are those of two single launches, bit for bit.
-constexpr int kTwoRing = 4;
-
+// interleaved `lag` tickets behind.  B(x, y) needs A of rows (x +- 1,
+// y +- 1); A(x, y) of a recycled ring slot needs B of the rows of planes
+// x - R - 1 .. x - R + 1 that read it.  With lag = (R + 1) ny / 2 + 2 both
+// kinds of wait are on tickets at least about (R - 3) ny / 2 earlier (the
+// slack the tickets in flight need before a wait becomes a stall), and every row a
+// ticket waits for has a smaller ticket (checked on the host for R 4..16
+// and a range of shapes with lag <= nx ny).  A waiting CTA reads the rows'
+// flags (the launch's epoch once the row is written) with acquire semantics,
+// one flag per lane of its first warp; a CTA publishes a row by a
+// __syncthreads, a fence and a release store of its flag.  The rows waited
+// for are held by CTAs that took their tickets earlier and are running (a
+// CTA takes its next ticket while it works on the current one, which still
+// leaves the smallest unfinished ticket free to proceed), so every wait
+// ends; each is bounded all the same, and one that runs out sets the error
+// flag and ends the CTA.  Ring values are read with ld.global.cg (L2, never
+// a stale L1 line of a recycled slot).  The cell arithmetic is k_step_fxs's,
+// fixed point in and out, so the results are those of two single launches,
+// bit for bit.
 __device__ __forceinline__ int ld_acquire(const int* p)
 {
     int v;
@@ -172,27 +176,51 @@ __device__ __forceinline__ void st_release(int* p, int v)
 }
 
 // Ring slot of x-plane x.
-__device__ __forceinline__ int two_slot(int x) { return x < 2 ? x : 2 + (x - 2) % kTwoRing; }
+__device__ __forceinline__ int two_slot(int x, int R) { return x < 2 ? x : 2 + (x - 2) % R; }
 
-template <bool OM_GE1>
-__global__ void __launch_bounds__(kStepBlock, 5)
+// L2 policy that keeps the ring's lines in L2 ahead of the streams of the
+// source and the destination.
+__device__ __forceinline__ uint64_t l2_keep_policy()
+{
+    uint64_t p;
+    asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+
+__device__ __forceinline__ uint64_t ld_ring(const unsigned long long* p, uint64_t pol)
+{
+    uint64_t v;
+    asm volatile("ld.global.cg.L2::cache_hint.u64 %0, [%1], %2;" : "=l"(v) : "l"(p), "l"(pol));
+    return v;
+}
+
+__device__ __forceinline__ void st_ring(unsigned long long* p, uint64_t v, uint64_t pol)
+{
+    asm volatile("st.global.cg.L2::cache_hint.u64 [%0], %1, %2;" ::"l"(p), "l"(v), "l"(pol) : "memory");
+}
+
+template <bool OM_GE1, int MINB>
+__global__ void __launch_bounds__(kStepBlock, MINB)
     k_two_fxs(const unsigned long long* __restrict__ src, unsigned long long* __restrict__ dst, Geom g, FxConst c,
               TwoStepCtl ts, int j, int* __restrict__ fail)
 {
-    __shared__ int s_ticket, s_abort;
+    __shared__ int s_next[2], s_abort;
     if (*fail < j) return;  // an earlier step of the run failed
-    const int nx = g.nx, ny = g.ny, nz = g.nz;
-    const int N = nx * ny, L = 2 * ny + 3, T = 2 * N;
-    const size_t mplane = (size_t)(kTwoRing + 2) * ny * nz;  // ring values per direction
+    const int nx = g.nx, ny = g.ny, nz = g.nz, R = ts.ring;
+    const int N = nx * ny, L = ts.lag, T = 2 * N;
+    const size_t mplane = (size_t)(R + 2) * ny * nz;  // ring values per direction
     unsigned long long* mid = ts.mid;
-    for (;;) {
-        if (threadIdx.x == 0) {
-            s_ticket = (int)atomicAdd(ts.counter, 1u);
-            s_abort = 0;
-        }
-        __syncthreads();
-        const int t = s_ticket;
-        if (t >= T) return;
+    const uint64_t keep = l2_keep_policy();
+    if (threadIdx.x == 0) {
+        s_next[0] = (int)atomicAdd(ts.counter, 1u);
+        s_abort = 0;
+    }
+    __syncthreads();
+    int t = s_next[0];
+    for (int it = 1; t < T; it ^= 1) {
+        // the next ticket, taken now so that its latency hides behind this row
+        int next = 0;
+        if (threadIdx.x == 0) next = (int)atomicAdd(ts.counter, 1u);
         // the ticket's phase and row
         bool isA;
         int r;
@@ -208,28 +236,29 @@ __global__ void __launch_bounds__(kStepBlock, 5)
             x = p < nx - 1 ? p + 1 : 0;
             y = q < ny - 1 ? q + 1 : 0;
         }
-        // wait for the rows this one reads (B) or whose ring slot it reuses (A)
-        if (threadIdx.x == 0) {
-            const int* flags = isA ? ts.flag_b : ts.flag_a;
-            const int x0 = isA ? x - kTwoRing - 1 : x - 1;
-            const bool needed = !isA || x >= kTwoRing + 2;
-            bool ok = true;
-            for (int dx = 0; dx < 3 && needed && ok; ++dx)
-                for (int dy = -1; dy <= 1 && ok; ++dy) {
-                    int xx = x0 + dx;
-                    xx = xx < 0 ? xx + nx : xx >= nx ? xx - nx : xx;
-                    int yy = y + dy;
-                    yy = yy < 0 ? yy + ny : yy >= ny ? yy - ny : yy;
-                    const int* f = flags + (size_t)xx * ny + yy;
-                    if (ld_acquire(f) == ts.epoch) continue;
-                    const long long t0 = clock64();
-                    while (ld_acquire(f) != ts.epoch)
-                        if (clock64() - t0 > ts.cycles) {
-                            ok = false;
-                            break;
-                        }
+        // wait for the rows this one reads (B) or whose ring slot it reuses (A):
+        // lane i of warp 0 watches row (x0 + i / 3, y - 1 + i % 3)
+        if (threadIdx.x < 32 && (!isA || x >= R + 2)) {
+            const int lane = threadIdx.x;
+            const int* f = nullptr;
+            if (lane < 9) {
+                int xx = (isA ? x - R - 1 : x - 1) + lane / 3;
+                xx = xx < 0 ? xx + nx : xx >= nx ? xx - nx : xx;
+                int yy = y - 1 + lane % 3;
+                yy = yy < 0 ? yy + ny : yy >= ny ? yy - ny : yy;
+                f = (isA ? ts.flag_b : ts.flag_a) + (size_t)xx * ny + yy;
+            }
+            const long long t0 = clock64();
+            bool timed_out = false;
+            for (;;) {
+                const bool mine = lane >= 9 || ld_acquire(f) == ts.epoch;
+                if (__all_sync(0xffffffffu, mine)) break;
+                if (__any_sync(0xffffffffu, clock64() - t0 > ts.cycles)) {
+                    timed_out = true;
+                    break;
                 }
-            if (!ok) {
+            }
+            if (timed_out && lane == 0) {
                 atomicOr(ts.err, 1u);
                 s_abort = 1;
             }
@@ -238,41 +267,43 @@ __global__ void __launch_bounds__(kStepBlock, 5)
         if (s_abort) return;
         const int xm = x == 0 ? nx - 1 : x - 1, xp = x == nx - 1 ? 0 : x + 1;
         const int ym = y == 0 ? ny - 1 : y - 1, yp = y == ny - 1 ? 0 : y + 1;
+        // source planes by e + 1 (the pull reads x - e): lattice planes for A, ring slots for B
+        const int ps[3] = {isA ? xp : two_slot(xp, R), isA ? x : two_slot(x, R), isA ? xm : two_slot(xm, R)};
         for (int k = threadIdx.x; k < nz; k += blockDim.x) {
             const int km = k == 0 ? nz - 1 : k - 1, kp = k == nz - 1 ? 0 : k + 1;
-            const int xs[3] = {xp, x, xm}, ys[3] = {yp, y, ym}, zs[3] = {kp, k, km};  // by e + 1: source x - e
+            const int ys[3] = {yp, y, ym}, zs[3] = {kp, k, km};
             uint64_t in[kQ], out[kQ];
             if (isA) {
 #pragma unroll
                 for (int a = 0; a < kQ; ++a)
                     in[a] = __ldg(src + (size_t)a * g.plane +
-                                  ((size_t)xs[ex(a, 0) + 1] * ny + ys[ex(a, 1) + 1]) * nz +
-                                  zs[ex(a, 2) + 1]);
+                                  ((size_t)ps[ex(a, 0) + 1] * ny + ys[ex(a, 1) + 1]) * nz + zs[ex(a, 2) + 1]);
             } else {
 #pragma unroll
                 for (int a = 0; a < kQ; ++a)
-                    in[a] = __ldcg(mid + (size_t)a * mplane +
-                                   ((size_t)two_slot(xs[ex(a, 0) + 1]) * ny + ys[ex(a, 1) + 1]) * nz +
-                                   zs[ex(a, 2) + 1]);
+                    in[a] = ld_ring(mid + (size_t)a * mplane +
+                                        ((size_t)ps[ex(a, 0) + 1] * ny + ys[ex(a, 1) + 1]) * nz + zs[ex(a, 2) + 1],
+                                    keep);
             }
             bool ok = true;
             fx::collide_cell_io<OM_GE1, true, true>(in, out, c, ok);
             if (isA) {
-                const size_t cell = ((size_t)two_slot(x) * ny + y) * nz + k;
+                const size_t cell = ((size_t)two_slot(x, R) * ny + y) * nz + k;
 #pragma unroll
-                for (int a = 0; a < kQ; ++a) __stcg(mid + (size_t)a * mplane + cell, out[a]);
+                for (int a = 0; a < kQ; ++a) st_ring(mid + (size_t)a * mplane + cell, out[a], keep);
             } else {
                 const size_t cell = ((size_t)x * ny + y) * nz + k;
 #pragma unroll
-                for (int a = 0; a < kQ; ++a) dst[(size_t)a * g.plane + cell] = out[a];
+                for (int a = 0; a < kQ; ++a) __stcs(dst + (size_t)a * g.plane + cell, out[a]);
             }
             if (!ok) atomicMin(fail, j);
         }
-        __syncthreads();  // every value of the row is stored
-        if (threadIdx.x == 0) {
-            __threadfence();
+        // s_next[it] was last read before this ticket's wait barrier
+        if (threadIdx.x == 0) s_next[it] = next;
+        __syncthreads();  // every value of the row is stored; the next ticket is shared
+        if (threadIdx.x == 0)  // release: cumulative over the CTA's stores ordered by the barrier
             st_release((isA ? ts.flag_a : ts.flag_b) + (size_t)x * ny + y, ts.epoch);
-        }
+        t = s_next[it];
     }
 }
 
@@ -383,22 +414,35 @@ cudaError_t launch_step_fx_run(const double* src, double* dst, const Geom& g, co
                      : launch_fxs<false>(in, out, g, fx.k, j, n, fail, s);
 }
 
-bool two_step_eligible(const Geom& g) { return g.nx >= kTwoRing + 4 && g.ny >= 4 && (size_t)g.nx * g.ny < (1u << 30); }
+int two_step_lag(const Geom& g, int ring) { return (ring + 1) * g.ny / 2 + 2; }
 
-size_t two_step_ring_values(const Geom& g) { return (size_t)kQ * (kTwoRing + 2) * g.ny * g.nz; }
+bool two_step_eligible(const Geom& g, int ring)
+{
+    return ring >= kTwoRingMin && ring <= kTwoRingMax && g.nx >= 8 && g.ny >= 4 && (size_t)g.nx * g.ny < (1u << 30) &&
+           (size_t)two_step_lag(g, ring) <= (size_t)g.nx * g.ny;
+}
+
+size_t two_step_ring_values(const Geom& g, int ring) { return (size_t)kQ * (ring + 2) * g.ny * g.nz; }
 
 cudaError_t launch_two_step_fx(const double* src, double* dst, const Geom& g, const FxParams& fx, const TwoStepCtl& ts,
-                               int j, int* fail, cudaStream_t s)
+                               int ctas_per_sm, int j, int* fail, cudaStream_t s)
 {
-    if (!two_step_eligible(g)) return cudaErrorInvalidValue;
+    if (!two_step_eligible(g, ts.ring) || ts.lag != two_step_lag(g, ts.ring) || ctas_per_sm < 1 || ctas_per_sm > 6)
+        return cudaErrorInvalidValue;
     cudaError_t e = cudaMemsetAsync(ts.counter, 0, sizeof(unsigned), s);
     if (e != cudaSuccess) return e;
-    // persistent: the CTAs that can be resident (5 per SM by the launch bounds)
-    const unsigned grid = (unsigned)(current_sm_count() * 5);
+    // persistent: at most the CTAs that can be resident (6 per SM: the
+    // instantiation held to 80 registers; up to 5: the one at 96)
+    const unsigned grid = (unsigned)(current_sm_count() * ctas_per_sm);
     const auto* in = reinterpret_cast<const unsigned long long*>(src);
     auto* out = reinterpret_cast<unsigned long long*>(dst);
-    if (fx.om_ge1) k_two_fxs<true><<<grid, kStepBlock, 0, s>>>(in, out, g, fx.k, ts, j, fail);
-    else k_two_fxs<false><<<grid, kStepBlock, 0, s>>>(in, out, g, fx.k, ts, j, fail);
+    if (ctas_per_sm == 6) {
+        if (fx.om_ge1) k_two_fxs<true, 6><<<grid, kStepBlock, 0, s>>>(in, out, g, fx.k, ts, j, fail);
+        else k_two_fxs<false, 6><<<grid, kStepBlock, 0, s>>>(in, out, g, fx.k, ts, j, fail);
+    } else {
+        if (fx.om_ge1) k_two_fxs<true, 5><<<grid, kStepBlock, 0, s>>>(in, out, g, fx.k, ts, j, fail);
+        else k_two_fxs<false, 5><<<grid, kStepBlock, 0, s>>>(in, out, g, fx.k, ts, j, fail);
+    }
     return cudaGetLastError();
 }
 

@@ -28,16 +28,20 @@ struct TwoStepCtl {
     int* flag_a;
     int* flag_b;
     unsigned long long* mid;
+    int ring;  // recycled x-planes of the ring (R)
+    int lag;   // tickets between the first A row and the first B row (two_step_lag)
     int epoch;
     long long cycles;
     unsigned* err;
 };
-bool two_step_eligible(const Geom& g);
-size_t two_step_ring_values(const Geom& g);
+constexpr int kTwoRingMin = 4, kTwoRingMax = 16, kTwoRingDefault = 12;
+int two_step_lag(const Geom& g, int ring);
+bool two_step_eligible(const Geom& g, int ring);
+size_t two_step_ring_values(const Geom& g, int ring);
 // Steps j and j + 1 of a fixed-point run (X in, X out; *fail as for
 // launch_step_fx_run, set to j if either step leaves the exact range).
 cudaError_t launch_two_step_fx(const double* src, double* dst, const Geom& g, const FxParams& fx, const TwoStepCtl& ts,
-                               int j, int* fail, cudaStream_t s);
+                               int ctas_per_sm, int j, int* fail, cudaStream_t s);
 // X on the float64 grid -> float64, in place, n values.
 cudaError_t launch_fx_to_f64(double* buf, size_t n, cudaStream_t s);
 struct RowConfig;

@@ -281,66 +281,44 @@ int time_fixed_run(imex_lattice* h, int reps, float* ms)
 
 int check_kernel_error(imex_lattice* h);
 
-// Resources of the two-steps-per-launch kernel (allocated once per handle):
-// the ticket counter, 2 nx ny row flags (zero: no epoch yet) and the ring.
-int ensure_two_step(imex_lattice* h)
+// Resources of the two-steps-per-launch kernel (per handle, grown to the
+// deepest ring a launch shape asks for): the ticket counter, 2 nx ny row
+// flags (zero: no epoch yet) and the ring of `ring` + 2 x-planes.
+int ensure_two_step(imex_lattice* h, int ring)
 {
-    if (h->two_mem) return IMEX_OK;
+    if (h->two_mem && h->two_ring >= ring) return IMEX_OK;
     const size_t rows = (size_t)h->g.nx * h->g.ny;
-    const size_t ring = two_step_ring_values(h->g) * sizeof(unsigned long long);
+    const size_t bytes = two_step_ring_values(h->g, ring) * sizeof(unsigned long long);
     const size_t head = (16 + 2 * rows * sizeof(int) + 255) & ~(size_t)255;
+    if (h->two_mem) {  // a shallower ring: its flags' epochs are kept by the new one's zeros
+        IMEX_CUDA(h, cudaFreeAsync(h->two_mem, h->stream), "cudaFreeAsync");
+        h->bytes -= h->two_bytes;
+        h->two_mem = nullptr;
+    }
     unsigned char* m = nullptr;
-    IMEX_CUDA(h, cudaMallocAsync((void**)&m, head + ring, h->stream), "cudaMallocAsync");
+    IMEX_CUDA(h, cudaMallocAsync((void**)&m, head + bytes, h->stream), "cudaMallocAsync");
     IMEX_CUDA(h, cudaMemsetAsync(m, 0, head, h->stream), "cudaMemset");
     h->two_mem = m;
+    h->two_ring = ring;
+    h->two_bytes = head + bytes;
     h->two.counter = reinterpret_cast<unsigned*>(m);
     h->two.flag_a = reinterpret_cast<int*>(m + 16);
     h->two.flag_b = h->two.flag_a + rows;
     h->two.mid = reinterpret_cast<unsigned long long*>(m + head);
     h->two.err = h->d_err;
-    h->bytes += head + ring;
+    h->bytes += h->two_bytes;
     return IMEX_OK;
 }
 
-// Steps j, j + 1 of a run in one launch of the two-step kernel.
-cudaError_t launch_two(imex_lattice* h, const double* src, double* dst, int j)
+// Steps j, j + 1 of a run in one launch of the two-step kernel, launch
+// shape rc (rows: ring depth, ctas_per_sm: resident CTAs).
+cudaError_t launch_two(imex_lattice* h, const RowConfig& rc, const double* src, double* dst, int j)
 {
+    h->two.ring = rc.rows;
+    h->two.lag = two_step_lag(h->g, rc.rows);
     h->two.epoch = ++h->two_epoch;
     h->two.cycles = make_wait_ctl(h->d_err).cycles;
-    return launch_two_step_fx(src, dst, h->g, h->fx, h->two, j, h->d_fail, h->stream);
-}
-
-// The two-steps-per-launch form of the run (stages 1): milliseconds per
-// step of `reps` launches from X in the spare buffer into a temporary third
-// buffer, as time_fixed_run times the one-step form.
-int time_two_run(imex_lattice* h, int reps, float* ms)
-{
-    int rc = ensure_two_step(h);
-    if (rc) return rc;
-    const size_t bytes = (size_t)kQ * h->ncells * sizeof(double);
-    double* tmp = nullptr;
-    IMEX_CUDA(h, cudaMallocAsync(&tmp, bytes, h->stream), "cudaMallocAsync");
-    double* x = dbuf(h, 1 - h->cur);
-    cudaEvent_t e0 = nullptr, e1 = nullptr;
-    const int n = 2 * reps + 2;
-    cudaError_t e = cudaMemsetAsync(h->d_fail, 0x7f, sizeof(int), h->stream);
-    if (e == cudaSuccess) e = launch_step_fx_run(dbuf(h, h->cur), x, h->g, h->fx, 1, n, h->d_fail, h->stream);
-    if (e == cudaSuccess) e = cudaEventCreate(&e0);
-    if (e == cudaSuccess) e = cudaEventCreate(&e1);
-    if (e == cudaSuccess) e = cudaEventRecord(e0, h->stream);
-    for (int r = 0; r < reps && e == cudaSuccess; ++r) e = launch_two(h, x, tmp, 2 + 2 * r);
-    if (e == cudaSuccess) e = cudaEventRecord(e1, h->stream);
-    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
-    float t = 0.f;
-    if (e == cudaSuccess) e = cudaEventElapsedTime(&t, e0, e1);
-    if (e0) cudaEventDestroy(e0);
-    if (e1) cudaEventDestroy(e1);
-    cudaError_t e2 = cudaFreeAsync(tmp, h->stream);
-    if (e == cudaSuccess) e = e2;
-    if (e != cudaSuccess) return cuda_fail(h, e, "autotune");
-    h->launches += reps + 1;
-    *ms = t / (2 * reps);
-    return check_kernel_error(h);
+    return launch_two_step_fx(src, dst, h->g, h->fx, h->two, rc.ctas_per_sm, j, h->d_fail, h->stream);
 }
 
 // Time every candidate in interleaved rounds (so that a drift of the clock
@@ -350,11 +328,6 @@ int tune(imex_lattice* h)
 {
     std::vector<RowConfig> cands = row_candidates(h);
     RowConfig best{};  // classic
-    if (use_fixed(h) && two_step_eligible(h->g)) {
-        RowConfig two{};
-        two.stages = 1;  // one thread per cell, two steps per launch
-        cands.insert(cands.begin(), two);
-    }
     if (!cands.empty()) {
         cands.insert(cands.begin(), RowConfig{});
         std::vector<float> fastest(cands.size(), 0.f);
@@ -362,9 +335,7 @@ int tune(imex_lattice* h)
             for (size_t c = 0; c < cands.size(); ++c) {
                 float ms = 0.f;
                 const int reps = round == 0 ? 1 : 4;  // round 0 warms up
-                int rc = cands[c].stages == 1 ? time_two_run(h, reps, &ms)
-                         : c == 0 && use_fixed(h) ? time_fixed_run(h, reps, &ms)
-                                                  : time_shape(h, cands[c], reps, &ms);
+                int rc = c == 0 && use_fixed(h) ? time_fixed_run(h, reps, &ms) : time_shape(h, cands[c], reps, &ms);
                 if (rc) return rc;
                 if (round == 1 || ms < fastest[c]) fastest[c] = ms;
             }
@@ -703,7 +674,7 @@ int step_fixed_run(imex_lattice* h, int n)
     std::vector<std::pair<int, int>> runs;
     const bool two = h->rows.stages == 1;  // two steps per launch where it can
     if (two) {
-        int rc = ensure_two_step(h);
+        int rc = ensure_two_step(h, h->rows.rows);
         if (rc) return rc;
     }
     IMEX_CUDA(h, cudaMemsetAsync(h->d_fail, 0x7f, sizeof(int), h->stream), "cudaMemset");
@@ -712,7 +683,7 @@ int step_fixed_run(imex_lattice* h, int n)
         runs.emplace_back(j, h->cur);
         // a pair holds fixed point in and out: not the run's first or last step
         const bool pair = two && j > 1 && j + 1 < n;
-        cudaError_t e = pair ? launch_two(h, dbuf(h, h->cur), dbuf(h, 1 - h->cur), j)
+        cudaError_t e = pair ? launch_two(h, h->rows, dbuf(h, h->cur), dbuf(h, 1 - h->cur), j)
                              : launch_step_fx_run(dbuf(h, h->cur), dbuf(h, 1 - h->cur), h->g, h->fx, j, n, h->d_fail,
                                                   h->stream);
         IMEX_CUDA(h, e, "step kernel launch");
@@ -1035,11 +1006,17 @@ int imex_set_launch(imex_lattice* h, int stages, int rows_per_stage, int ctas_pe
         return IMEX_OK;
     }
     if (stages == 0 || stages == 1) {
-        if (stages == 1 && !(use_fixed(h) && two_step_eligible(h->g)))
-            return fail(h, IMEX_ERR_ARG, "imex_set_launch: two steps per launch (stages 1) needs the float64 fixed-point "
-                                         "engine and nx >= 8, ny >= 4");
-        h->rows = RowConfig{};
-        h->rows.stages = stages;
+        RowConfig rc{};
+        rc.stages = stages;
+        if (stages == 1) {  // rows_per_stage: ring depth; ctas_per_sm: resident CTAs
+            rc.rows = rows_per_stage >= kTwoRingMin ? rows_per_stage : kTwoRingDefault;
+            rc.ctas_per_sm = ctas_per_sm < 1 ? 5 : ctas_per_sm;
+            if (!(use_fixed(h) && two_step_eligible(h->g, rc.rows)) || rc.ctas_per_sm > 6)
+                return fail(h, IMEX_ERR_ARG, "imex_set_launch: two steps per launch (stages 1) needs the float64 "
+                                             "fixed-point engine, nx >= 8, ny >= 4, a ring of 4..16 planes whose lag "
+                                             "fits in the lattice and 1..6 CTAs per SM");
+        }
+        h->rows = rc;
         h->shape_mode = 0;
         h->shape_pinned = true;
         return IMEX_OK;
@@ -1077,7 +1054,7 @@ int imex_get_launch(imex_lattice* h, int out[4])
     int rc = ensure_tuned(h);
     if (rc) return rc;
     out[0] = h->rows.stages;
-    out[1] = h->rows.stages > 1 ? h->rows.rows : 0;
+    out[1] = h->rows.stages >= 1 ? h->rows.rows : 0;  // two steps per launch: the ring depth
     out[2] = h->rows.ctas_per_sm;
     out[3] = h->rows.stages > 1 ? h->rows.threads : kStepBlock;  // one thread per cell: blocks of kStepBlock
     return IMEX_OK;

@@ -53,6 +53,8 @@ struct imex_lattice {
     // two fused steps per launch (launch_two_step_fx): ticket counter, row
     // flags of both phases and the L2-resident ring, allocated on first use
     unsigned char* two_mem = nullptr;
+    int two_ring = 0;        // ring depth two_mem holds
+    size_t two_bytes = 0;
     imex::TwoStepCtl two{};
     int two_epoch = 0;
     int fx_backoff = 0;         // calls skipped after the last failure (doubles per failure, up to 64)

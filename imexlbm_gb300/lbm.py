@@ -187,8 +187,10 @@ class LBM:
 
     def set_launch(self, stages: int, rows_per_stage: int = 1, ctas_per_sm: int = 1) -> None:
         """Pin the fused step's launch shape (stages 0: one thread per cell;
-        >= 2: row-staged ring depth, with rows_per_stage y-rows per item and
-        ctas_per_sm resident CTAs; < 0: automatic)."""
+        1: two steps per launch through a ring of rows_per_stage + 2 x-planes,
+        ctas_per_sm resident CTAs - float64 fixed point only, never chosen
+        automatically; >= 2: row-staged ring depth, with rows_per_stage
+        y-rows per item and ctas_per_sm resident CTAs; < 0: automatic)."""
         self._check(self._L.imex_set_launch(self._h, int(stages), int(rows_per_stage), int(ctas_per_sm)))
 
     def get_launch(self):

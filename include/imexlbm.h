@@ -230,11 +230,16 @@ int imex_conserved_noalloc(const double *f_dev, int nx, int ny, int nz, double *
 
 /* Launch shape of the fused step.  stages = 0: one thread per cell pulling
  * straight from global memory.  stages = 1 (float64 fixed-point engine, nx
- * >= 8, ny >= 4): the same, with imex_step's runs taking two steps per
- * launch - the first step's values go to a ring of x-planes small enough to
- * stay in L2 and the second step reads them there, rows ordered across the
- * GPU by tickets and per-row flags (bounded waits); the numbers are the
- * one-step form's, bit for bit.  stages >= 2: the row-staged kernel - each
+ * >= 8, ny >= 4; only when pinned, the automatic choice never takes it):
+ * the same, with imex_step's runs taking two steps per launch - the first
+ * step's values go to a ring of rows_per_stage + 2 x-planes in device
+ * memory (rows_per_stage 4..16, below 4: 12) and the second step reads
+ * them there, rows ordered across the GPU by tickets and per-row flags
+ * (bounded waits), ctas_per_sm 1..6 resident CTAs (below 1: 5); the
+ * numbers are the one-step form's, bit for bit, and it runs slower than
+ * stages 0 on GB300 (10-30% at 128^3-256^3, more on small lattices).
+ * imex_get_launch reports the ring depth as rows_per_stage.
+ * stages >= 2: the row-staged kernel - each
  * CTA keeps a ring of `stages` work items in shared memory, an item being
  * rows_per_stage consecutive y-rows (dividing ny for float64; for reduced
  * precision the last item of a plane takes the rows left) whose 27 source row runs

@@ -285,16 +285,19 @@ def test_get_f_leaves_the_streaming_pending(imex):
         assert lat.kernel_launches() - before == 1
 
 
-@pytest.mark.parametrize("shape", [(32, 32, 32), (9, 5, 7), (8, 4, 16), (17, 19, 23), (12, 40, 33)])
-def test_two_steps_per_launch_equal_single_steps(imex, oracle, shape):
+@pytest.mark.parametrize("shape,ring,ctas", [((32, 32, 32), 4, 5), ((32, 32, 32), 16, 6), ((9, 5, 7), 4, 1),
+                                             ((8, 4, 16), 6, 2), ((17, 19, 23), 12, 5), ((12, 40, 33), 8, 6)])
+def test_two_steps_per_launch_equal_single_steps(imex, oracle, shape, ring, ctas):
     """Runs of two fused steps per launch (launch shape stages 1: the first
-    step's values through the L2-resident ring of x-planes, rows ordered by
-    tickets and flags) give the one-step run's numbers bit for bit, odd and
-    even step counts, and stay within 1e-12 of the oracle."""
+    step's values through the ring of x-planes, rows ordered by tickets and
+    flags) give the one-step run's numbers bit for bit, odd and even step
+    counts, for ring depths 4..16 and both CTA residencies, and stay within
+    1e-12 of the oracle."""
     tau = 0.004
     with imex.LBM(*shape, tau, 1.0, 0.05, engine=imex.IMEX_ENGINE_FIXED) as a, \
             imex.LBM(*shape, tau, 1.0, 0.05, engine=imex.IMEX_ENGINE_FIXED) as b:
-        a.set_launch(1, 1, 1)
+        a.set_launch(1, ring, ctas)
+        assert a.get_launch()[:3] == (1, ring, ctas)
         b.set_launch(0, 1, 1)
         for lat in (a, b):
             lat.Initialize()
@@ -332,6 +335,11 @@ def test_two_step_shape_is_refused_where_it_does_not_apply(imex):
     with imex.LBM(6, 8, 8, 0.01, 1.0, 0.05) as lat:        # nx < 8
         with pytest.raises(imex.ImexError):
             lat.set_launch(1, 1, 1)
+    with imex.LBM(8, 4, 8, 0.01, 1.0, 0.05) as lat:        # the lag of a 16-plane ring exceeds nx * ny
+        lat.set_launch(1, 4, 5)
+        for bad in ((1, 16, 5), (1, 17, 5), (1, 4, 7)):
+            with pytest.raises(imex.ImexError):
+                lat.set_launch(*bad)
     with imex.LBM(16, 16, 16, 0.01, 1.0, 0.05, precision=imex.IMEX_F32) as lat:
         with pytest.raises(imex.ImexError):
             lat.set_launch(1, 1, 1)
