@@ -430,17 +430,20 @@ def run_ours(a):
     # fixed-point engine's run of steps: k_step_fxs, whose first and last
     # launches read / write float64)
     hbm, peak_kind = load_peaks()
-    launch_ms = ms / max(1, gpu_launches)
     bpc = BYTES_PER_CELL[a.precision]
-    achieved = bpc * cells / (launch_ms * 1e-3) / 1e9
+    # algorithmic bytes per step over the time per step (a launch is one step,
+    # or two for the pinned two-steps-per-launch shape)
+    achieved = bpc * cells * a.steps / (ms * 1e-3) / 1e9
     kname = {"fixed": "step_fxs", "native": "step_f64", "float32": "step_lowp_" + a.precision}[eng_name]
+    if eng_name == "fixed" and launch_shape[0] == 1:
+        kname = "two_fxs"
     tr, tr_size = load_traffic(kname)
     roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
             "frac": round(achieved / hbm, 4), "peak_kind": peak_kind,
             "traffic": round(tr * cells, 0) if tr is not None else None,
             "traffic_from": (f"ncu dram bytes per cell of a {tr_size} capture ({tr} B), times this launch's "
                              f"{cells} cells (profiles/dram_traffic.json)") if tr is not None else None,
-            "kernel": kname, "algorithmic_bytes_per_launch": bpc * cells}
+            "kernel": kname, "algorithmic_bytes_per_launch": bpc * cells * (2 if kname == "two_fxs" else 1)}
 
     # end-to-end through the public API with host buffers
     e2e = None

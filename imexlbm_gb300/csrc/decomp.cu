@@ -14,18 +14,19 @@
 // machines/aurora/README.md:79-82, and the unused d_dirset of src/lbm.hpp:153).
 //
 // Sub-domains (device).  Each block keeps its distributions in a padded box
-// f[a][Lx+2][Ly+2][Lz+2] with a one-cell ghost shell (the reference keeps 3
-// ghost layers and fills one, src/mpi_view_transfer.cpp:197-200).  The state
-// machine is the single lattice's: the buffers hold C(f) with the streaming
-// pending, so a step is
-//   1. the halo exchange - one kernel fills every block's ghost shell from
-//      its neighbours' boundary cells, the pruned directions of each channel
-//      only: the one-GPU image of pack_f / exchange_f / unpack_f
-//      (src/mpi_view_transfer.cpp:260-456), whose peer reads would be peer
-//      loads over NVLink on a multi-GPU machine;
-//   2. per block the fused pull + collision (the fixed-point engine's cell
-//      arithmetic, native float64 for cells outside its range), reading the
-//      ghost shell where the pull leaves the block.
+// f[a][Lx+2][Ly+2][P] with a one-cell ghost shell (the reference keeps 3
+// ghost layers and fills one, src/mpi_view_transfer.cpp:197-200; P pads a
+// z-row so that its interior starts on a 32-byte sector).  The state machine
+// is the single lattice's: the buffers hold C(f) with the streaming pending,
+// and a step is one launch over every block of the fused pull + collision
+// (the fixed-point engine's cell arithmetic; runs of steps hold the state as
+// fixed point between launches, as the undivided lattice's do), reading the
+// ghost shell where the pull leaves the block.  The halo exchange is part of
+// the same launch: a boundary cell's new values that leave its block - the
+// pruned directions of each channel only - are stored straight into the
+// ghost shell of the block they stream into (push_halo), the one-GPU image
+// of pack_f / exchange_f / unpack_f (src/mpi_view_transfer.cpp:260-456),
+// whose sends would be peer stores over NVLink on a multi-GPU machine.
 // Collision is per cell and streaming a permutation, so every f is bit-
 // identical to the undivided lattice's whatever the decomposition
 // (tests/test_decomp_gpu.py); only the order of the conserved sums differs,
@@ -42,6 +43,7 @@
 #include "imexlbm.h"
 #include "imexlbm_internal.hpp"
 #include "kernels_f64.cuh"
+#include "kernels_fx.cuh"
 #include "tg_init.cuh"
 
 namespace imex {
@@ -165,63 +167,95 @@ int check_plan_args(int nranks, int nx, int ny, int nz, const char* what, Plan* 
 
 constexpr int kThreads = 128;
 
-// A block's padded box: interior extents and values per direction plane,
-// (Lx+2)(Ly+2)(Lz+2).
+// A block's padded box: interior extents L, the z pitch P of a row and the
+// values per direction plane, (Lx+2)(Ly+2)P.  Padded z coordinate k (0: the
+// ghost below, 1..Lz: interior, Lz+1: the ghost above) sits at kZOff + k in
+// its row; with P a multiple of 4 the interior of every row starts on a
+// 32-byte sector, so a warp's 32 values are 8 whole sectors.
+constexpr int kZOff = 3;
 struct PadGeom {
     int L[3];
+    int P;
     size_t plane;
 };
 
-// One block on the device (the halo kernel's table).
+inline int pad_pitch(int Lz) { return (Lz + 2 + kZOff + 3) & ~3; }
+
+// One block on the device: its buffers, geometry and the block next to it
+// at each offset (ox, oy, oz) in {-1, 0, 1}^3 (periodic; itself along an axis
+// the grid does not split), entry (ox + 1) 9 + (oy + 1) 3 + (oz + 1).
 struct BlockDev {
     double* buf[2];
     PadGeom g;
+    int nb[27];
 };
 
 __host__ __device__ inline size_t pad_index(const PadGeom& b, int i, int j, int k)
 {
-    return ((size_t)i * (b.L[1] + 2) + j) * (b.L[2] + 2) + k;
+    return ((size_t)i * (b.L[1] + 2) + j) * b.P + kZOff + k;
 }
 
-// A contiguous box of ghost cells of block `dst` and the boundary box of
-// block `src` it copies, for the directions `dirs` (a channel's message).
-struct HaloSeg {
-    unsigned long long begin;  // first work item (value) of the segment
-    int dst, src;
-    int dst0[3], src0[3], ext[3];
-    int ndir;
-    int dirs[9];
-};
-
-constexpr int kMaxSegs = 26 * 512;
-
-// The halo exchange of every block in one launch: work item q of a segment
-// is (direction, x, y, z) of its box, z fastest; it copies one value from the
-// source block's boundary into the destination block's ghost shell, both in
-// buffer `cur`.
-__global__ void __launch_bounds__(256) k_halo(const HaloSeg* __restrict__ segs, int nsegs, unsigned long long total,
-                                              const BlockDev* __restrict__ blocks, int cur)
+// The halo exchange, as stores from the producer.  When a step (or the
+// first in-place collision) has the new values of a cell on its block's
+// boundary, every value whose direction leaves the block - 9 through a face,
+// 3 more through each edge, 1 through a corner: the reference's channels
+// pruned to the directions that cross them - is also stored into the ghost
+// shell of the block it streams into, at the ghost cell the next pull of
+// that block reads (padded coordinate 0 when it enters the neighbour from
+// below, L + 1 from above, unchanged along an axis it does not cross).  No
+// exchange kernel, no pack buffer and no re-read of the boundary: on several
+// GPUs these are the peer stores over NVLink that replace pack_f /
+// exchange_f / unpack_f (src/mpi_view_transfer.cpp:260-456).  Interior
+// cell (i, j, k) of block `self` (0-based), values v, ghost shells of
+// buffer `buf`.
+template <typename T>
+__device__ __forceinline__ void push_halo(const BlockDev* __restrict__ blocks, int self, int buf, const PadGeom& g,
+                                          int i, int j, int k, const T (&v)[kQ])
 {
-    for (unsigned long long q = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; q < total;
-         q += (unsigned long long)gridDim.x * blockDim.x) {
-        int lo = 0, hi = nsegs;  // largest lo with segs[lo].begin <= q
-        while (hi - lo > 1) {
-            const int mid = (lo + hi) >> 1;
-            if (segs[mid].begin <= q) lo = mid;
-            else hi = mid;
+    const bool hx = i == g.L[0] - 1, lx = i == 0, hy = j == g.L[1] - 1, ly = j == 0, hz = k == g.L[2] - 1, lz = k == 0;
+    const int faces = (int)hx + (int)lx + (int)hy + (int)ly + (int)hz + (int)lz;
+    if (faces == 0) return;
+    const int* nb = blocks[self].nb;
+    if (faces == 1) {  // on one face only (most boundary cells): one neighbour, 9 values
+        const int axis = (hx || lx) ? 0 : (hy || ly) ? 1 : 2;
+        const int side = (hx || hy || hz) ? 1 : -1;
+        const int o = axis == 0 ? (side + 1) * 9 + 4 : axis == 1 ? 9 + (side + 1) * 3 + 1 : 13 + side;
+        const BlockDev& N = blocks[__ldg(&nb[o])];
+        PadGeom ng;
+        ng.L[0] = __ldg(&N.g.L[0]);
+        ng.L[1] = __ldg(&N.g.L[1]);
+        ng.L[2] = __ldg(&N.g.L[2]);
+        ng.P = __ldg(&N.g.P);
+        ng.plane = __ldg(&N.g.plane);
+        int t[3] = {i + 1, j + 1, k + 1};
+        t[axis] = side == 1 ? 0 : ng.L[axis] + 1;
+        const size_t base = pad_index(ng, t[0], t[1], t[2]);
+        T* dst = reinterpret_cast<T*>(N.buf[buf]);
+#pragma unroll
+        for (int a = 0; a < kQ; ++a) {
+            const int e = axis == 0 ? ex(a, 0) : axis == 1 ? ex(a, 1) : ex(a, 2);
+            if (e == side) dst[(size_t)a * ng.plane + base] = v[a];
         }
-        const HaloSeg& s = segs[lo];
-        unsigned long long r = q - s.begin;
-        const int k = (int)(r % (unsigned)s.ext[2]);
-        r /= (unsigned)s.ext[2];
-        const int j = (int)(r % (unsigned)s.ext[1]);
-        r /= (unsigned)s.ext[1];
-        const int i = (int)(r % (unsigned)s.ext[0]);
-        const int a = s.dirs[r / (unsigned)s.ext[0]];
-        const BlockDev& D = blocks[s.dst];
-        const BlockDev& S = blocks[s.src];
-        D.buf[cur][(size_t)a * D.g.plane + pad_index(D.g, s.dst0[0] + i, s.dst0[1] + j, s.dst0[2] + k)] =
-            S.buf[cur][(size_t)a * S.g.plane + pad_index(S.g, s.src0[0] + i, s.src0[1] + j, s.src0[2] + k)];
+        return;
+    }
+#pragma unroll
+    for (int a = 0; a < kQ; ++a) {
+        const int ox = (hx && ex(a, 0) == 1) ? 1 : (lx && ex(a, 0) == -1) ? -1 : 0;
+        const int oy = (hy && ex(a, 1) == 1) ? 1 : (ly && ex(a, 1) == -1) ? -1 : 0;
+        const int oz = (hz && ex(a, 2) == 1) ? 1 : (lz && ex(a, 2) == -1) ? -1 : 0;
+        if (ox == 0 && oy == 0 && oz == 0) continue;
+        const BlockDev& N = blocks[__ldg(&nb[(ox + 1) * 9 + (oy + 1) * 3 + (oz + 1)])];
+        PadGeom ng;
+        ng.L[0] = __ldg(&N.g.L[0]);
+        ng.L[1] = __ldg(&N.g.L[1]);
+        ng.L[2] = __ldg(&N.g.L[2]);
+        ng.P = __ldg(&N.g.P);
+        ng.plane = __ldg(&N.g.plane);
+        const int tx = ox == 1 ? 0 : ox == -1 ? ng.L[0] + 1 : i + 1;
+        const int ty = oy == 1 ? 0 : oy == -1 ? ng.L[1] + 1 : j + 1;
+        const int tz = oz == 1 ? 0 : oz == -1 ? ng.L[2] + 1 : k + 1;
+        T* dst = reinterpret_cast<T*>(N.buf[buf]);
+        dst[(size_t)a * ng.plane + pad_index(ng, tx, ty, tz)] = v[a];
     }
 }
 
@@ -233,14 +267,42 @@ __device__ __forceinline__ size_t pull_at(const PadGeom& b, int I, int J, int K)
     return (size_t)A * b.plane + pad_index(b, I - ex(A, 0), J - ex(A, 1), K - ex(A, 2));
 }
 
-template <int A = 0>
-__device__ __forceinline__ void gather_pad(const double* __restrict__ src, const PadGeom& b, int I, int J, int K,
-                                           double (&f)[kQ])
+template <int A = 0, typename T>
+__device__ __forceinline__ void gather_pad(const T* __restrict__ src, const PadGeom& b, int I, int J, int K,
+                                           T (&f)[kQ])
 {
     if constexpr (A < kQ) {
         f[A] = __ldg(src + pull_at<A>(b, I, J, K));
         gather_pad<A + 1>(src, b, I, J, K, f);
     }
+}
+
+// Interior cell of a launch over every block (grid x: row segments of
+// kThreads z-cells of the largest block, grid y: block): the block's
+// geometry and padded coordinates (I, J, K) of this thread's cell; false
+// for a thread past its block's cells.
+struct DomCell {
+    PadGeom g;
+    int I, J, K;
+};
+
+__device__ __forceinline__ bool dom_cell(const BlockDev* __restrict__ blocks, DomCell& c)
+{
+    const BlockDev& B = blocks[blockIdx.y];
+    c.g.L[0] = __ldg(&B.g.L[0]);
+    c.g.L[1] = __ldg(&B.g.L[1]);
+    c.g.L[2] = __ldg(&B.g.L[2]);
+    c.g.P = __ldg(&B.g.P);
+    c.g.plane = __ldg(&B.g.plane);
+    const int nzs = (c.g.L[2] + kThreads - 1) / kThreads;
+    const unsigned r = blockIdx.x / (unsigned)nzs;
+    const int zs = (int)(blockIdx.x - r * (unsigned)nzs);
+    const int j = (int)(r % (unsigned)c.g.L[1]), i = (int)(r / (unsigned)c.g.L[1]);
+    const int k = zs * kThreads + threadIdx.x;
+    c.I = i + 1;
+    c.J = j + 1;
+    c.K = k + 1;
+    return i < c.g.L[0] && k < c.g.L[2];
 }
 
 __device__ __forceinline__ void load_cell(const double* __restrict__ src, const PadGeom& b, int I, int J, int K,
@@ -266,17 +328,18 @@ __global__ void __launch_bounds__(kThreads) k_dom_init(double* __restrict__ f, P
     for (int a = 0; a < kQ; ++a) f[(size_t)a * b.plane + c] = fe[a];
 }
 
-// In-place collision of the interior (the first Collision() of a run), with
-// the undivided lattice's arithmetic: fixed point, native float64 for a
-// cell outside its exact range.
+// In-place collision of every block's interior (the first Collision() of a
+// run), with the undivided lattice's arithmetic: fixed point, native
+// float64 for a cell outside its exact range.
 template <bool OM_GE1>
-__global__ void __launch_bounds__(kThreads, 5) k_dom_collide(double* __restrict__ f, PadGeom b, FxConst c,
+__global__ void __launch_bounds__(kThreads, 5) k_dom_collide(const BlockDev* __restrict__ blocks, int cur, FxConst c,
                                                             CollideF64 cp, unsigned long long* __restrict__ fallback)
 {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, i = blockIdx.z;
-    if (k >= b.L[2]) return;
+    DomCell dc;
+    if (!dom_cell(blocks, dc)) return;
+    double* f = blocks[blockIdx.y].buf[cur];
     double v[kQ], out[kQ];
-    load_cell(f, b, i + 1, j + 1, k + 1, v);
+    load_cell(f, dc.g, dc.I, dc.J, dc.K, v);
     bool ok = true;
     fx::collide_cell<OM_GE1>(v, out, c, ok);
     if (!ok) {
@@ -285,41 +348,78 @@ __global__ void __launch_bounds__(kThreads, 5) k_dom_collide(double* __restrict_
         for (int a = 0; a < kQ; ++a) out[a] = v[a];
         atomicAdd(fallback, 1ull);
     }
-    const size_t cell = pad_index(b, i + 1, j + 1, k + 1);
+    const size_t cell = pad_index(dc.g, dc.I, dc.J, dc.K);
 #pragma unroll
-    for (int a = 0; a < kQ; ++a) f[(size_t)a * b.plane + cell] = out[a];
+    for (int a = 0; a < kQ; ++a) f[(size_t)a * dc.g.plane + cell] = out[a];
+    // the ghost shells of this buffer are not read by this kernel
+    push_halo(blocks, blockIdx.y, cur, dc.g, dc.I - 1, dc.J - 1, dc.K - 1, out);
 }
 
-// Native float64 redo of one cell outside the fixed-point range.
-__device__ __noinline__ void dom_fallback(const double* __restrict__ src, double* __restrict__ dst, PadGeom b, int I,
-                                          int J, int K, CollideF64 cp, unsigned long long* fallback)
+// Native float64 redo of one cell outside the fixed-point range (its
+// stores, halo included, replace the ones the caller made).
+__device__ __noinline__ void dom_fallback(const BlockDev* __restrict__ blocks, int cur, PadGeom b, int I, int J, int K,
+                                          CollideF64 cp, unsigned long long* fallback)
 {
+    const double* src = blocks[blockIdx.y].buf[cur];
+    double* dst = blocks[blockIdx.y].buf[1 - cur];
     double v[kQ];
     gather_pad(src, b, I, J, K, v);
     collide_f64(v, cp);
     const size_t c = pad_index(b, I, J, K);
 #pragma unroll
     for (int a = 0; a < kQ; ++a) dst[(size_t)a * b.plane + c] = v[a];
+    push_halo(blocks, blockIdx.y, 1 - cur, b, I - 1, J - 1, K - 1, v);
     atomicAdd(fallback, 1ull);
 }
 
-// Fused pull + collision of a block's interior from buffer cur into 1 - cur;
-// the pull reads the ghost shell where it leaves the block.
+// Fused pull + collision of every block's interior from buffer cur into
+// 1 - cur, float64 in and out; the pull reads the ghost shell where it
+// leaves the block.
 template <bool OM_GE1>
-__global__ void __launch_bounds__(kThreads, 5) k_dom_step(const double* __restrict__ src, double* __restrict__ dst,
-                                                         PadGeom b, FxConst c, CollideF64 cp,
-                                                         unsigned long long* __restrict__ fallback)
+__global__ void __launch_bounds__(kThreads, 5) k_dom_step(const BlockDev* __restrict__ blocks, int cur, FxConst c,
+                                                         CollideF64 cp, unsigned long long* __restrict__ fallback)
 {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, i = blockIdx.z;
-    if (k >= b.L[2]) return;
+    DomCell dc;
+    if (!dom_cell(blocks, dc)) return;
+    const double* src = blocks[blockIdx.y].buf[cur];
+    double* dst = blocks[blockIdx.y].buf[1 - cur];
     double f[kQ], out[kQ];
-    gather_pad(src, b, i + 1, j + 1, k + 1, f);
+    gather_pad(src, dc.g, dc.I, dc.J, dc.K, f);
     bool ok = true;
     fx::collide_cell<OM_GE1>(f, out, c, ok);
-    const size_t cell = pad_index(b, i + 1, j + 1, k + 1);
+    const size_t cell = pad_index(dc.g, dc.I, dc.J, dc.K);
 #pragma unroll
-    for (int a = 0; a < kQ; ++a) dst[(size_t)a * b.plane + cell] = out[a];
-    if (!ok) dom_fallback(src, dst, b, i + 1, j + 1, k + 1, cp, fallback);
+    for (int a = 0; a < kQ; ++a) dst[(size_t)a * dc.g.plane + cell] = out[a];
+    push_halo(blocks, blockIdx.y, 1 - cur, dc.g, dc.I - 1, dc.J - 1, dc.K - 1, out);
+    if (!ok) dom_fallback(blocks, cur, dc.g, dc.I, dc.J, dc.K, cp, fallback);
+}
+
+// The same step inside a run of steps holding the state as fixed point X on
+// the float64 grid between launches (IN_FX / OUT_FX: X instead of float64),
+// the undivided lattice's k_step_fxs: a cell outside the exact range records
+// step j in *fail, later launches of the run return at once, and the host
+// redoes the run from the last complete step with k_dom_step.
+template <bool OM_GE1, bool IN_FX, bool OUT_FX>
+__global__ void __launch_bounds__(kThreads, 5) k_dom_run(const BlockDev* __restrict__ blocks, int cur, FxConst c, int j,
+                                                        int* __restrict__ fail)
+{
+    if (*fail < j) return;  // an earlier step of the run failed
+    DomCell dc;
+    if (!dom_cell(blocks, dc)) return;
+    const auto* src = reinterpret_cast<const unsigned long long*>(blocks[blockIdx.y].buf[cur]);
+    auto* dst = reinterpret_cast<unsigned long long*>(blocks[blockIdx.y].buf[1 - cur]);
+    unsigned long long f[kQ];
+    gather_pad(src, dc.g, dc.I, dc.J, dc.K, f);
+    uint64_t in[kQ], out[kQ];
+#pragma unroll
+    for (int a = 0; a < kQ; ++a) in[a] = f[a];
+    bool ok = true;
+    fx::collide_cell_io<OM_GE1, IN_FX, OUT_FX>(in, out, c, ok);
+    const size_t cell = pad_index(dc.g, dc.I, dc.J, dc.K);
+#pragma unroll
+    for (int a = 0; a < kQ; ++a) dst[(size_t)a * dc.g.plane + cell] = out[a];
+    push_halo(blocks, blockIdx.y, 1 - cur, dc.g, dc.I - 1, dc.J - 1, dc.K - 1, out);
+    if (!ok) atomicMin(fail, j);
 }
 
 // A block's f (pulled through the pending streaming when PULL) into the
@@ -382,6 +482,16 @@ dim3 block_grid(const BlockDev& b)
     return dim3((unsigned)((b.g.L[2] + kThreads - 1) / kThreads), (unsigned)b.g.L[1], (unsigned)b.g.L[0]);
 }
 
+// Grid of a launch over every block (dom_cell): the largest block's row
+// segments by the block count.
+dim3 domain_grid(const std::vector<BlockDev>& dev)
+{
+    size_t most = 0;
+    for (const BlockDev& b : dev)
+        most = std::max(most, (size_t)b.g.L[0] * b.g.L[1] * ((b.g.L[2] + kThreads - 1) / kThreads));
+    return dim3((unsigned)most, (unsigned)dev.size(), 1);
+}
+
 }  // namespace
 }  // namespace imex
 
@@ -392,12 +502,12 @@ struct imex_domain {
     std::vector<imex_block> blocks;
     std::vector<BlockDev> dev;     // host copy of the device table
     BlockDev* d_blocks = nullptr;
-    HaloSeg* d_segs = nullptr;
-    int nsegs = 0;
     unsigned long long halo_values = 0;  // values the halo exchange moves per step
     double* d_partial = nullptr;   // conserved partial sums, then 5 sums per block
     size_t partials = 0;           // partials per block region (largest block)
     unsigned long long* d_fallback = nullptr;
+    int* d_fail = nullptr;         // first failing step of a fixed-point run
+    int fx_skip = 0, fx_backoff = 0;  // after a failed run: calls that step one at a time
     double* d_field = nullptr;     // whole-lattice staging for imex_domain_get_f (lazily)
     cudaStream_t stream = nullptr;
     int device = 0;
@@ -440,53 +550,97 @@ int ready(imex_domain* d, const char* what)
     return IMEX_OK;
 }
 
-int halo(imex_domain* d)
-{
-    if (!d->halo_values) return IMEX_OK;
-    int sms = current_sm_count();
-    const unsigned long long want = (d->halo_values + 255) / 256;
-    const unsigned grid = (unsigned)std::min<unsigned long long>(want, (unsigned long long)sms * 8);
-    k_halo<<<grid, 256, 0, d->stream>>>(d->d_segs, d->nsegs, d->halo_values, d->d_blocks, d->cur);
-    D_CUDA(d, cudaGetLastError(), "halo kernel launch");
-    ++d->launches;
-    return IMEX_OK;
-}
-
 // First Collision of a run: in place, the streaming then pending (the
 // undivided lattice's imex_collision on an exact state).
 int collide_exact(imex_domain* d)
 {
-    for (const BlockDev& b : d->dev) {
-        if (d->fx.om_ge1)
-            k_dom_collide<true><<<block_grid(b), kThreads, 0, d->stream>>>(b.buf[d->cur], b.g, d->fx.k, d->cf64,
-                                                                          d->d_fallback);
-        else
-            k_dom_collide<false><<<block_grid(b), kThreads, 0, d->stream>>>(b.buf[d->cur], b.g, d->fx.k, d->cf64,
-                                                                           d->d_fallback);
-        D_CUDA(d, cudaGetLastError(), "collision kernel launch");
-        ++d->launches;
-    }
+    const dim3 grid = domain_grid(d->dev);
+    if (d->fx.om_ge1)
+        k_dom_collide<true><<<grid, kThreads, 0, d->stream>>>(d->d_blocks, d->cur, d->fx.k, d->cf64, d->d_fallback);
+    else
+        k_dom_collide<false><<<grid, kThreads, 0, d->stream>>>(d->d_blocks, d->cur, d->fx.k, d->cf64, d->d_fallback);
+    D_CUDA(d, cudaGetLastError(), "collision kernel launch");
+    ++d->launches;
     d->tag = 2;
     ++d->steps;
     return IMEX_OK;
 }
 
+// One fused step, float64 in and out, cells outside the fixed-point range
+// redone in native float64.
 int fused_step(imex_domain* d)
 {
-    int rc = halo(d);
-    if (rc) return rc;
-    for (const BlockDev& b : d->dev) {
-        const double* src = b.buf[d->cur];
-        double* dst = b.buf[1 - d->cur];
-        if (d->fx.om_ge1)
-            k_dom_step<true><<<block_grid(b), kThreads, 0, d->stream>>>(src, dst, b.g, d->fx.k, d->cf64, d->d_fallback);
-        else
-            k_dom_step<false><<<block_grid(b), kThreads, 0, d->stream>>>(src, dst, b.g, d->fx.k, d->cf64, d->d_fallback);
-        D_CUDA(d, cudaGetLastError(), "step kernel launch");
-        ++d->launches;
-    }
+    const dim3 grid = domain_grid(d->dev);
+    if (d->fx.om_ge1)
+        k_dom_step<true><<<grid, kThreads, 0, d->stream>>>(d->d_blocks, d->cur, d->fx.k, d->cf64, d->d_fallback);
+    else
+        k_dom_step<false><<<grid, kThreads, 0, d->stream>>>(d->d_blocks, d->cur, d->fx.k, d->cf64, d->d_fallback);
+    D_CUDA(d, cudaGetLastError(), "step kernel launch");
+    ++d->launches;
     d->cur = 1 - d->cur;
     ++d->steps;
+    return IMEX_OK;
+}
+
+template <bool OM_GE1>
+cudaError_t launch_run(imex_domain* d, int j, int n)
+{
+    const dim3 grid = domain_grid(d->dev);
+    const bool in_fx = j > 1, out_fx = j < n;
+    auto* b = d->d_blocks;
+    if (in_fx && out_fx) k_dom_run<OM_GE1, true, true><<<grid, kThreads, 0, d->stream>>>(b, d->cur, d->fx.k, j, d->d_fail);
+    else if (in_fx) k_dom_run<OM_GE1, true, false><<<grid, kThreads, 0, d->stream>>>(b, d->cur, d->fx.k, j, d->d_fail);
+    else if (out_fx) k_dom_run<OM_GE1, false, true><<<grid, kThreads, 0, d->stream>>>(b, d->cur, d->fx.k, j, d->d_fail);
+    else k_dom_run<OM_GE1, false, false><<<grid, kThreads, 0, d->stream>>>(b, d->cur, d->fx.k, j, d->d_fail);
+    return cudaGetLastError();
+}
+
+// n fused steps as one run holding the state as fixed point between its
+// launches (the undivided lattice's rule: float64 before and after, the
+// same bits as n single steps).  A cell leaving the exact range stops the
+// run at that step; the state before it is converted back to float64 and
+// the rest is stepped one at a time with the native fallback, and the next
+// 1, 2, 4 .. 64 calls (doubling per failure) step one at a time as well.
+int fused_run(imex_domain* d, int n)
+{
+    if (n < 2 || d->fx_skip > 0) {
+        if (n > 0 && d->fx_skip > 0) --d->fx_skip;
+        for (int s = 0; s < n; ++s) {
+            int rc = fused_step(d);
+            if (rc) return rc;
+        }
+        return IMEX_OK;
+    }
+    const int64_t steps0 = d->steps;
+    std::vector<int> src_of(n + 1);
+    D_CUDA(d, cudaMemsetAsync(d->d_fail, 0x7f, sizeof(int), d->stream), "cudaMemset");
+    for (int j = 1; j <= n; ++j) {
+        D_CUDA(d, d->fx.om_ge1 ? launch_run<true>(d, j, n) : launch_run<false>(d, j, n), "step kernel launch");
+        ++d->launches;
+        src_of[j] = d->cur;
+        d->cur = 1 - d->cur;
+        ++d->steps;
+    }
+    int failed = 0;
+    D_CUDA(d, cudaMemcpyAsync(&failed, d->d_fail, sizeof failed, cudaMemcpyDeviceToHost, d->stream), "cudaMemcpy");
+    D_CUDA(d, cudaStreamSynchronize(d->stream), "fixed-point run");
+    if (failed > n) {
+        d->fx_backoff = 0;
+        return IMEX_OK;
+    }
+    d->fx_backoff = d->fx_backoff ? std::min(64, 2 * d->fx_backoff) : 1;
+    d->fx_skip = d->fx_backoff;
+    d->cur = src_of[failed];
+    d->steps = steps0 + failed - 1;
+    if (failed > 1)
+        for (const BlockDev& b : d->dev) {
+            D_CUDA(d, launch_fx_to_f64(b.buf[d->cur], (size_t)kQ * b.g.plane, d->stream), "conversion");
+            ++d->launches;
+        }
+    for (int s = failed; s <= n; ++s) {
+        int rc = fused_step(d);
+        if (rc) return rc;
+    }
     return IMEX_OK;
 }
 
@@ -536,9 +690,9 @@ void imex_domain_destroy(imex_domain* d)
         for (double* p : b.buf)
             if (p) cudaFree(p);
     if (d->d_blocks) cudaFree(d->d_blocks);
-    if (d->d_segs) cudaFree(d->d_segs);
     if (d->d_partial) cudaFree(d->d_partial);
     if (d->d_fallback) cudaFree(d->d_fallback);
+    if (d->d_fail) cudaFree(d->d_fail);
     if (d->d_field) cudaFree(d->d_field);
     if (d->stream) cudaStreamDestroy(d->stream);
     delete d;
@@ -582,7 +736,8 @@ int imex_domain_create(int nx, int ny, int nz, int nranks, double tau, double rh
         block_of(p, r, &d->blocks[r]);
         BlockDev& b = d->dev[r];
         for (int q = 0; q < 3; ++q) b.g.L[q] = d->blocks[r].len[q];
-        b.g.plane = (size_t)(b.g.L[0] + 2) * (b.g.L[1] + 2) * (b.g.L[2] + 2);
+        b.g.P = pad_pitch(b.g.L[2]);
+        b.g.plane = (size_t)(b.g.L[0] + 2) * (b.g.L[1] + 2) * b.g.P;
         need += 2 * (size_t)kQ * b.g.plane * sizeof(double);
         const dim3 g = block_grid(b);
         d->partials = std::max(d->partials, (size_t)g.x * g.y * g.z);
@@ -597,37 +752,26 @@ int imex_domain_create(int nx, int ny, int nz, int nranks, double tau, double rh
             if (e == cudaSuccess) e = cudaMemsetAsync(ptr, 0, (size_t)kQ * b.g.plane * sizeof(double), d->stream);
             if (e != cudaSuccess) return bail(IMEX_ERR_MEMORY, "imex_domain_create: device allocation failed");
         }
-    // halo segments: block r's ghost box of channel c comes from the block
-    // behind it (recv_from) - that block's boundary box of the same channel
-    std::vector<HaloSeg> segs;
+    // each block's neighbours, and the values the halo moves per step: the
+    // pruned directions of every channel's box
     unsigned long long total = 0;
-    for (int r = 0; r < nranks; ++r)
-        for (int c = 0; c < 26; ++c) {
-            imex_halo_msg m, src;
-            halo_msg(p, r, c, &m);
-            halo_msg(p, m.recv_from, c, &src);
-            HaloSeg s{};
-            s.begin = total;
-            s.dst = r;
-            s.src = m.recv_from;
-            for (int q = 0; q < 3; ++q) {
-                s.dst0[q] = m.recv_lo[q];
-                s.src0[q] = src.send_lo[q];
-                s.ext[q] = m.ext[q];
-            }
-            s.ndir = m.ndir;
-            for (int q = 0; q < 9; ++q) s.dirs[q] = m.dirs[q];
-            total += (unsigned long long)s.ndir * s.ext[0] * s.ext[1] * s.ext[2];
-            segs.push_back(s);
+    for (int r = 0; r < nranks; ++r) {
+        for (int o = 0; o < 27; ++o) {
+            const int off[3] = {o / 9 - 1, (o / 3) % 3 - 1, o % 3 - 1};
+            d->dev[r].nb[o] = neighbour(p, d->blocks[r], off);
         }
-    d->nsegs = (int)segs.size();
+        for (int c = 0; c < 26; ++c) {
+            imex_halo_msg m;
+            halo_msg(p, r, c, &m);
+            total += (unsigned long long)m.ndir * m.ext[0] * m.ext[1] * m.ext[2];
+        }
+    }
     d->halo_values = total;
-    e = cudaMalloc(&d->d_segs, sizeof(HaloSeg) * segs.size());
-    if (e == cudaSuccess) e = cudaMemcpy(d->d_segs, segs.data(), sizeof(HaloSeg) * segs.size(), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMalloc(&d->d_blocks, sizeof(BlockDev) * nranks);
+    e = cudaMalloc(&d->d_blocks, sizeof(BlockDev) * nranks);
     if (e == cudaSuccess) e = cudaMemcpy(d->d_blocks, d->dev.data(), sizeof(BlockDev) * nranks, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMalloc(&d->d_partial, (d->partials + 1) * 5 * sizeof(double) * nranks);
     if (e == cudaSuccess) e = cudaMalloc(&d->d_fallback, sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMalloc(&d->d_fail, sizeof(int));
     if (e == cudaSuccess) e = cudaMemsetAsync(d->d_fallback, 0, sizeof(unsigned long long), d->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(d->stream);
     if (e != cudaSuccess) return bail(IMEX_ERR_CUDA, std::string("imex_domain_create: ") + cudaGetErrorString(e));
@@ -679,11 +823,12 @@ int imex_domain_step(imex_domain* d, int nsteps)
     int rc = ready(d, "imex_domain_step");
     if (rc) return rc;
     if (nsteps < 0) return dfail(d, IMEX_ERR_ARG, "imex_domain_step: nsteps < 0");
-    for (int s = 0; s < nsteps; ++s) {
-        rc = d->tag == 1 ? collide_exact(d) : fused_step(d);
+    if (nsteps > 0 && d->tag == 1) {
+        rc = collide_exact(d);
         if (rc) return rc;
+        --nsteps;
     }
-    return IMEX_OK;
+    return fused_run(d, nsteps);
 }
 
 int imex_domain_conserved_blocks(imex_domain* d, double* out)
@@ -691,11 +836,7 @@ int imex_domain_conserved_blocks(imex_domain* d, double* out)
     int rc = ready(d, "imex_domain_conserved");
     if (rc) return rc;
     if (!out) return dfail(d, IMEX_ERR_ARG, "imex_domain_conserved: null output");
-    const bool pull = d->tag == 2;
-    if (pull) {
-        rc = halo(d);
-        if (rc) return rc;
-    }
+    const bool pull = d->tag == 2;  // the ghost shells are current (the producers stored them)
     const size_t nb = d->dev.size();
     double* sums = d->d_partial + nb * d->partials * 5;
     for (size_t r = 0; r < nb; ++r) {
@@ -737,11 +878,7 @@ int imex_domain_get_f(imex_domain* d, double* host, size_t n)
     if (rc) return rc;
     const size_t cells = (size_t)d->plan.n[0] * d->plan.n[1] * d->plan.n[2];
     if (!host || n != (size_t)kQ * cells) return dfail(d, IMEX_ERR_ARG, "imex_domain_get_f: buffer size must be 27*nx*ny*nz");
-    const bool pull = d->tag == 2;
-    if (pull) {
-        rc = halo(d);
-        if (rc) return rc;
-    }
+    const bool pull = d->tag == 2;  // the ghost shells are current (the producers stored them)
     if (!d->d_field) D_CUDA(d, cudaMalloc(&d->d_field, n * sizeof(double)), "cudaMalloc");
     for (size_t r = 0; r < d->dev.size(); ++r) {
         const imex_block& b = d->blocks[r];

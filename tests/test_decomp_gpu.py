@@ -106,3 +106,22 @@ def test_domain_state_and_argument_errors(imex):
         imex.Domain(4, 4, 4, 5, 0.01, 1.0, 0.05)   # the grid puts 5 blocks along 4 cells
     with pytest.raises(imex.ImexError):
         imex.Domain(8, 8, 8, 2, 0.01, 2.0, 0.05)   # density outside the fixed-point range
+
+
+def test_run_leaving_the_fixed_point_range_is_redone(imex):
+    """A decomposed run whose cells leave the fixed-point engine's exact range
+    partway (a deck that diverges) is redone from the last complete step in
+    native float64: every f equals the undivided lattice stepped one step at
+    a time, NaNs included, and later calls keep agreeing."""
+    shape, tau, u0 = (16, 16, 16), 1e-4, 0.18
+    with imex.LBM(*shape, tau, 1.0, u0, engine=imex.IMEX_ENGINE_FIXED) as lat, \
+            imex.Domain(*shape, 4, tau, 1.0, u0) as dom:
+        lat.Initialize()
+        dom.Initialize()
+        for n in (40, 3, 7):
+            for _ in range(n):
+                lat.step(1)
+            dom.step(n)
+            assert np.array_equal(dom.get_f(), lat.get_f(), equal_nan=True), n
+        assert dom.fallback_cells() > 0
+        assert dom.info()["steps"] == 50
