@@ -484,11 +484,13 @@ int imex_decomp_halo(int nranks, int nx, int ny, int nz, int rank, int channel, 
  * as the reference's ranks step theirs (no counterpart as one object: the
  * reference runs one block per MPI rank).  Each block keeps float64
  * distributions in a padded box with a one-cell ghost shell; a step is one
- * halo-exchange kernel for all blocks (the pruned messages above, read from
- * the neighbours' memory) and one fused pull + collision kernel per block
- * (the fixed-point engine's arithmetic, so 0.75 <= rho0 <= 1.25).  Every f
- * equals the undivided lattice's bit for bit; the conserved sums are the
- * blocks' sums added in rank order. */
+ * fused pull + collision launch over every block (the fixed-point engine's
+ * arithmetic, so 0.75 <= rho0 <= 1.25; runs of steps in fixed point, as
+ * imex_step's) that also stores each boundary cell's outgoing values - the
+ * pruned directions of the messages above - into the ghost shells of the
+ * blocks they stream into: the halo exchange as the producer's stores.
+ * Every f equals the undivided lattice's bit for bit; the conserved sums are
+ * the blocks' sums added in rank order. */
 typedef struct imex_domain imex_domain;
 typedef struct imex_domain_stats {
     int nranks;
