@@ -219,15 +219,15 @@ def time_reference_build(n: int, nz: int, interval: int):
     deck = f"1.0 0.1 1600\n0.05 {2 * interval} {interval}\n{n} {n} {nz}\n"
     with tempfile.TemporaryDirectory() as d:
         t0 = time.perf_counter()
-        text = o.run_ref(deck, d, ranks=1, threads=cores, mode="main", timeout=1200)
+        text = o.run_ref(deck, d, ranks=1, threads=cores, mode="main", timeout=1200, bind=True)
         wall = time.perf_counter() - t0
     mlups = o.parse_mlups(text)
     if len(mlups) < 2:
         raise RuntimeError("the reference's run printed no second interval:\n" + text[-1000:])
     return {"value": mlups[1], "unit": "MLUPS", "cores": cores, "kind": "reference",
             "sample": f"the reference's src/*.cpp (unmodified, single-process Kokkos/MPI stand-ins, OpenMP "
-                      f"{cores} threads, 1 rank) on a {n}x{n}x{nz} lattice: its own MLUPS over the second "
-                      f"{interval}-step report interval of {2 * interval} steps",
+                      f"{cores} threads bound as its job scripts bind them, 1 rank) on a {n}x{n}x{nz} lattice: "
+                      f"its own MLUPS over the second {interval}-step report interval of {2 * interval} steps",
             "seconds": interval * n * n * nz / (mlups[1] * 1e6), "wall_s": wall}
 
 

@@ -181,16 +181,23 @@ def build_ref(refsrc: str | None = None) -> str | None:
 
 
 def run_ref(deck: str, cwd: str, ranks: int = 1, threads: int | None = None, mode: str = "main",
-            args: tuple = (), timeout: float = 600.0) -> str:
+            args: tuple = (), timeout: float = 600.0, bind: bool = False) -> str:
     """Run the reference's code on `ranks` rank threads in directory cwd
-    (which gets the deck as input.in); returns its standard output."""
+    (which gets the deck as input.in); returns its standard output.  bind:
+    OpenMP threads spread over the hardware threads and pinned there
+    (OMP_PROC_BIND=spread, OMP_PLACES=threads unless the environment sets
+    them), as the reference's job scripts run it (machines/polaris/env.sh:67-68)."""
     with open(os.path.join(cwd, "input.in"), "w") as fp:
         fp.write(deck)
     cmd = [REF_EXE, "--ranks", str(ranks)]
     if threads:
         cmd += ["--threads", str(threads)]
     cmd += [mode, *map(str, args)]
-    r = subprocess.run(cmd, cwd=cwd, capture_output=True, text=True, timeout=timeout)
+    env = dict(os.environ)
+    if bind:
+        env.setdefault("OMP_PROC_BIND", "spread")
+        env.setdefault("OMP_PLACES", "threads")
+    r = subprocess.run(cmd, cwd=cwd, capture_output=True, text=True, timeout=timeout, env=env)
     if r.returncode != 0:
         raise RuntimeError(f"imexref failed ({r.returncode}): {r.stderr[-2000:]}")
     return r.stdout
