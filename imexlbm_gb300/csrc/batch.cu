@@ -212,9 +212,19 @@ __global__ void __launch_bounds__(TPB, MINB)
     }
 }
 
+// Bytes of the row kernel's table of first items for `members` members.
+__host__ __device__ inline size_t rows_table_bytes(int members)
+{
+    return (sizeof(unsigned) * (size_t)(members + 1) + 15) & ~(size_t)15;
+}
+
 // Row-staged batched step (rows_lowp.cuh): work items of every member in
 // one persistent loop; an item's member is found by binary search over the
-// members' first-item indices, kept in shared memory after the ring.
+// members' first-item indices, kept in shared memory after the ring, and
+// its entry is copied next to them.  Thread 0 describes every item (it arms
+// the stage), ahead of the CTA barrier that ends the item before it; a
+// CTA's consecutive items usually belong to one member, so the entry is
+// looked up and loaded from global memory only when the member changes.
 template <int kDirBytes, int kMinBlocks>
 __global__ void __launch_bounds__(rowslp::kThreads, kMinBlocks)
     k_batch_rows(const RowsHeader* __restrict__ hdr, const BatchEntry* __restrict__ tab, int s, CollideF32 base,
@@ -228,20 +238,28 @@ __global__ void __launch_bounds__(rowslp::kThreads, kMinBlocks)
     }
     const unsigned total = hdr->total;
     unsigned* sbegin = reinterpret_cast<unsigned*>(smem + rowslp::smem_bytes(kDirBytes, stages));
+    BatchEntry* sentry = reinterpret_cast<BatchEntry*>(reinterpret_cast<unsigned char*>(sbegin) +
+                                                       rows_table_bytes(table_cap));
     for (int q = threadIdx.x; q < count; q += blockDim.x) sbegin[q] = tab[q].ibegin;
     if (threadIdx.x == 0) sbegin[count] = total;
     __syncthreads();
     const unsigned G = gridDim.x;
     const int my = blockIdx.x < total ? (int)((total - 1 - blockIdx.x) / G) + 1 : 0;
+    int cached = -1;  // member whose entry sentry holds (thread 0, the only caller)
     auto item_of = [&](int t) {
         const unsigned itx = blockIdx.x + (unsigned)t * G;
-        int lo = 0, hi = count;  // largest lo with sbegin[lo] <= itx
-        while (hi - lo > 1) {
-            const int mid = (lo + hi) >> 1;
-            if (sbegin[mid] <= itx) lo = mid;
-            else hi = mid;
+        if (cached < 0 || itx < sbegin[cached] || itx >= sbegin[cached + 1]) {
+            int lo = 0, hi = count;  // largest lo with sbegin[lo] <= itx
+            while (hi - lo > 1) {
+                const int mid = (lo + hi) >> 1;
+                if (sbegin[mid] <= itx) lo = mid;
+                else hi = mid;
+            }
+            *sentry = tab[lo];
+            cached = lo;
         }
-        const BatchEntry& e = tab[lo];
+        const BatchEntry& e = *sentry;
+        const int lo = cached;
         rowslp::Item it;
         const int cur = e.cur ^ (s & 1);
         it.src = static_cast<const unsigned char*>(e.buf[cur]);
@@ -345,12 +363,13 @@ CollideF32 base_constants()
     return make_collide_f32(0.0);
 }
 
-// Shared memory of a row-kernel CTA: barriers, ring and the table of the
-// members' first items, sized for the batch's capacity - a CUDA graph keeps
-// the size it was captured with while members join.
+// Shared memory of a row-kernel CTA: barriers, ring, the table of the
+// members' first items (sized for the batch's capacity - a CUDA graph keeps
+// the size it was captured with while members join) and a copy of the
+// member entry last looked up.
 size_t rows_smem(const RowShape& rs, int members)
 {
-    return rowslp::smem_bytes(rs.dir_kb * 1024, rs.stages) + ((sizeof(unsigned) * (members + 1) + 15) & ~15ull);
+    return rowslp::smem_bytes(rs.dir_kb * 1024, rs.stages) + rows_table_bytes(members) + sizeof(BatchEntry);
 }
 
 // Whether the row shape's CTAs fit an SM's shared memory.

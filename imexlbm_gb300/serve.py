@@ -13,8 +13,8 @@ Reported: p50 / p99 / max time-to-result (submission to result, queueing
 included), the aggregate MLUPS over the run, the batch's own MLUPS while
 busy, the peak number of requests in flight, and checks on sampled
 requests - the kinetic-energy error of the served result against the same
-solve in float64 alone (whose wall time, create to result, also gives the
-plain float64 path's MLUPS on the sample), and that the served result
+solve in float64 alone (whose steps, timed after its launch shape is tuned,
+also give the plain float64 path's MLUPS on the sample), and that the served result
 equals the same request run alone in its own precision, bit for bit.
 
 The offered load (about 1.9 M cells x 2600 steps per request, 50 per
@@ -69,12 +69,21 @@ def tau_of(edge, re, u0):
 PREC = {"f32": _lib.IMEX_F32, "f16dev": _lib.IMEX_F16DEV}
 
 
-def run_alone(req, precision):
+def run_alone(req, precision, timed=False):
+    """One request on its own lattice: its diagnostics, and with timed the
+    seconds of its steps alone (the launch shape tuned before them, creation,
+    initialisation and the diagnostics outside)."""
     with LBM(req["edge"], req["edge"], req["edge"], tau_of(req["edge"], req["Re"], req["u0"]), 1.0, req["u0"],
              precision=precision) as lat:
         lat.Initialize()
+        lat.get_launch()
+        lat.fence()
+        t0 = time.perf_counter()
         lat.step(req["steps"])
-        return lat.Conserved(allow_nonfinite=True)
+        lat.fence()
+        seconds = time.perf_counter() - t0
+        cons = lat.Conserved(allow_nonfinite=True)
+    return (cons, seconds) if timed else cons
 
 
 def run(rate=50.0, duration=60.0, budget_gb=120.0, max_active=256, steps_per_tick=25, spot=16, seed=20261203,
@@ -138,9 +147,8 @@ def run(rate=50.0, duration=60.0, budget_gb=120.0, max_active=256, steps_per_tic
     for k in sample:
         r = ok[k]
         req = reqs[r["tag"]]
-        t0 = time.perf_counter()
-        ref64 = run_alone(req, _lib.IMEX_F64)      # the plain float64 path, one request at a time
-        f64_seconds += time.perf_counter() - t0
+        ref64, sec = run_alone(req, _lib.IMEX_F64, timed=True)  # the plain float64 path, one request at a time
+        f64_seconds += sec
         f64_updates += r["cells"] * r["steps"]
         err = abs(r["conserved"][4] - ref64[4]) / ref64[4]
         ke_err.append(err)

@@ -10,7 +10,8 @@ Default workload: 512^3, Re = 1600, u0 = 0.05, 2000 steps, reporting every
 Every report step prints, for (b) and (c) against (a): the relative
 kinetic-energy error, the largest velocity difference over all cells (in
 units of u0) and the relative mass drift of each run; at the end, each
-run's MLUPS (CUDA events around its own steps) and the worst errors.
+run's MLUPS (CUDA events around its own steps, each lattice's launch shape
+tuned before the first) and the worst errors.
 Mass, momentum and ke are float64 reductions in every run.
 
 Usage: python -m imexlbm_gb300.sweep [--size 512] [--steps 2000] [--report 100]
@@ -42,6 +43,7 @@ def run(size=512, steps=2000, report=100, re=1600, u0=0.05, out=None, log=print)
         lat.set_stream(streams[name].cuda_stream)
         lat.set_rounding(_lib.IMEX_ROUND_STOCHASTIC if name.endswith("_sr") else _lib.IMEX_ROUND_NEAREST)
         lat.Initialize()
+        lat.get_launch()  # the launch-shape autotuner, outside the timed steps (it leaves the state as it is)
         lats[name] = lat
     m0 = {k: v.Conserved()[0] for k, v in lats.items()}
     ms = {k: 0.0 for k in lats}
