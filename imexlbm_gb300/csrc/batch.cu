@@ -331,6 +331,7 @@ struct imex_batch {
     int graph_k = 0;
     BatchShape graph_shape;
     unsigned long long graph_units = 0;  // segments the captured cell-kernel launches cover
+    const int* graph_group = nullptr;    // the group table the captured segment-kernel launches read
     RowShape graph_rshape;
     int graph_kinds = 0;  // bit 0: cell kernel, bit 1: row kernel, bit 2: cell kernel with float16 members
     int64_t launches = 0;
@@ -742,9 +743,14 @@ int capture_graph(imex_batch* b, int K)
     b->graph_rshape = b->rshape;
     b->graph_kinds = kinds(b);
     b->graph_units = b->h_hdr->total;
+    b->graph_group = b->d_group;
     return IMEX_OK;
 }
 
+// Whether the captured graph still describes the launches: the same shapes
+// and kernels, and for the segment kernel the same segment count (its grid)
+// and the same group table (a pointer baked into the graph; upload_table
+// moves the table when a tick or a tuning candidate needs a larger one).
 bool graph_valid(const imex_batch* b, int K)
 {
     return b->graph && b->graph_k == K && b->graph_shape.threads == b->shape.threads &&
@@ -752,7 +758,7 @@ bool graph_valid(const imex_batch* b, int K)
            b->graph_rshape.stages == b->rshape.stages && b->graph_rshape.dir_kb == b->rshape.dir_kb &&
            b->graph_rshape.f32 == b->rshape.f32 &&
            b->graph_rshape.ctas_per_sm == b->rshape.ctas_per_sm && b->graph_kinds == kinds(b) &&
-           (b->shape.cpt != 0 || b->n_cell == 0 || b->graph_units == b->h_hdr->total);
+           (b->shape.cpt != 0 || b->n_cell == 0 || (b->graph_units == b->h_hdr->total && b->graph_group == b->d_group));
 }
 
 }  // namespace

@@ -232,3 +232,30 @@ def test_segment_kernel_graph_follows_the_members(imex):
         assert b.get_launch() == (128, 0, 0)
     for lat in lats:
         lat.close()
+
+
+def test_segment_kernel_graph_after_a_retune_moves_its_group_table(imex):
+    """A re-tune times the row kernel switched off, which puts every member
+    in the segment kernel; when that outgrows the segment kernel's group
+    table, the table moves.  A graph captured before reads the table through
+    a pointer baked into it, so it must be captured again even when the
+    tuner settles on the same shapes and the segment count is the one it
+    was captured with; every member still ends where it ends alone."""
+    specs = [((16, 16, 16), "f32", 0.004, 0.05, (0.0, 0.0, 0.0)),
+             ((64, 64, 16), "f16dev", 0.02, 0.06, (0.3, 1.1, 2.0)),
+             ((96, 96, 16), "f16dev", 0.01, 0.07, (2.5, 0.1, 4.0))]
+    lats = [make(imex, s) for s in specs]
+    with imex.Batch(4) as b:
+        b.set_graph(4)
+        for lat in lats[:2]:
+            b.add(lat)
+        b.step(8)                      # tuned with the float32 member in the segment kernel, graph captured
+        b.add(lats[2])
+        b.step(4)                      # a larger float16 member joins the row kernel
+        b.set_launch(0, 0, 0)          # re-tune both kernels: a row-kernel-off candidate
+        b.set_row_launch(0, 0, 0, 1)   # needs more groups than the table holds
+        b.step(8)
+        for lat, s in zip(lats, specs):
+            assert np.array_equal(lat.get_f(), alone(imex, s, lat.steps_done()))
+    for lat in lats:
+        lat.close()
