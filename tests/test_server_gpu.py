@@ -165,3 +165,32 @@ def test_least_work_policy_admits_small_requests_first(imex):
     assert got[3]["t_admit"] < got[2]["t_admit"]
     with pytest.raises(imex.ImexError):
         imex.Server(budget_bytes=1e8, max_active=1, steps_per_tick=5).set_policy(7)
+
+
+def test_results_survive_retunes_as_the_batch_grows_and_shrinks(imex):
+    """Large float16 requests joining a running float32 / float16 pair
+    multiply the batch's cells, so the server re-tunes its launch shapes
+    (and again when they leave); a re-tune times the row kernel switched
+    off, which outgrows the segment kernel's group table.  The tick's
+    captured graph must follow, and every result equal the request alone."""
+    reqs = [(16, 0.004, 0.05, 300, "f32"), (32, 0.02, 0.06, 300, "f16dev"),
+            (96, 0.01, 0.07, 40, "f16dev"), (80, 0.003, 0.05, 35, "f16dev"), (24, 0.002, 0.08, 30, "f32")]
+    with imex.Server(budget_bytes=4e9, max_active=8, steps_per_tick=5) as srv:
+        got = {}
+        for i, r in enumerate(reqs):
+            edge, tau, u0, steps, pname = r
+            srv.submit(edge, edge, edge, tau, u0, steps, prec(imex, pname), tag=i)
+            if i == 1:  # let the first two run (tuned, graph captured) before the large ones arrive
+                t0 = time.time()
+                while srv.stats()["ticks"] < 3 and time.time() - t0 < 60:
+                    time.sleep(0.005)
+        t0 = time.time()
+        while len(got) < len(reqs) and time.time() - t0 < 120:
+            for res in srv.poll():
+                got[res["tag"]] = res
+            time.sleep(0.01)
+        st = srv.stats()
+    assert len(got) == len(reqs) and st["failed"] == 0
+    for i, r in enumerate(reqs):
+        assert got[i]["status"] == 0, got[i]
+        assert got[i]["conserved"] == alone(imex, r), i
