@@ -125,3 +125,21 @@ def test_run_leaving_the_fixed_point_range_is_redone(imex):
             assert np.array_equal(dom.get_f(), lat.get_f(), equal_nan=True), n
         assert dom.fallback_cells() > 0
         assert dom.info()["steps"] == 50
+
+
+@pytest.mark.parametrize("nranks,n", [(8, (2, 2, 2)), (27, (3, 3, 3)), (16, (4, 4, 4)), (6, (3, 2, 6)), (9, (3, 3, 9))])
+def test_blocks_one_cell_thick(imex, nranks, n):
+    """Blocks one cell thick along an axis: a cell on both faces of that axis
+    stores its values into both neighbours' ghost shells (and, on a 1x1x1
+    block, into every neighbour's); every f still equals the undivided
+    lattice's, over runs of odd and even length."""
+    tau, u0 = 0.01, 0.05
+    with imex.LBM(*n, tau, 1.0, u0) as lat, imex.Domain(*n, nranks, tau, 1.0, u0) as dom:
+        assert min(min(imex.decomp_block(nranks, *n, r)["len"]) for r in range(nranks)) == 1
+        lat.Initialize()
+        dom.Initialize()
+        for k in (1, 4, 7, 2):
+            lat.step(k)
+            dom.step(k)
+            assert np.array_equal(dom.get_f(), lat.get_f()), k
+        assert dom.fallback_cells() == 0
