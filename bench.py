@@ -22,7 +22,7 @@ one reference time step (collision + pull streaming) of the whole lattice.
 --impl reference times that build of the reference on the full 256^3
 lattice (its own MLUPS line of a bounded report interval).
 
-Multi-GPU: the path does not shard on a one-GPU machine; under torchrun each
+Multi-GPU: the path does not shard on one GPU; under torchrun each
 rank advances its own independent lattice (replicas, weak scaling) and
 value = all ranks' cell updates / the slowest rank's time.
 """

@@ -26,7 +26,7 @@
 // pruned directions of each channel only - are stored straight into the
 // ghost shell of the block they stream into (push_halo), the one-GPU image
 // of pack_f / exchange_f / unpack_f (src/mpi_view_transfer.cpp:260-456),
-// whose sends would be peer stores over NVLink on a multi-GPU machine.
+// whose sends would be peer stores over NVLink across several GPUs.
 // Collision is per cell and streaming a permutation, so every f is bit-
 // identical to the undivided lattice's whatever the decomposition
 // (tests/test_decomp_gpu.py); only the order of the conserved sums differs,

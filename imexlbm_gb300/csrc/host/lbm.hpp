@@ -53,7 +53,7 @@ struct LBM {
 
     LBM(int sx, int sy, int sz, double& tau, double& rho0, double& u0, int precision = IMEX_F64);
     // Same argument list as the reference (lbm.hpp:179): the communicator is
-    // ignored because this build runs one lattice per process.
+    // ignored: one lattice per process, on one GPU.
     template <class Comm>
     LBM(Comm, int sx, int sy, int sz, double& tau, double& rho0, double& u0, int precision = IMEX_F64)
         : LBM(sx, sy, sz, tau, rho0, u0, precision)

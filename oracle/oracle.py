@@ -1,7 +1,7 @@
 """ctypes wrapper around the CPU oracle (test infrastructure only).
 
-The oracle is the checker for the CUDA library: tests, the smoke check and the
-benchmark's CPU-baseline leg may call it; the product path never does.  It
+The oracle is what the CUDA library is checked against: tests, the smoke check
+and the benchmark's CPU-baseline leg may call it; the product path never does.  It
 restates the reference's single-rank IMEXLBM step in plain C (see the header
 of ``lbm_oracle.c`` for the reference file:line of every function).
 

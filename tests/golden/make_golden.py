@@ -2,8 +2,8 @@
 
 The reference (Maccchiatooo/IMEXLBM) ships no field dumps; its known answers
 for the time step live as text in tests/regression.sh and input.in.  This
-script reads those files (it is run in a container where the reference is
-mounted; the GPU machine never reads the reference) and writes:
+script reads those files (it runs where the reference's checkout is present;
+the tests read only the fixtures it writes) and writes:
 
   regression_known_answers.json   deck, tolerances, ke trajectory and the
                                   measured residual scale of tests/regression.sh

@@ -29,7 +29,7 @@ def make(imex, shape, tau, rho0=1.0, u0=0.05, engine="native"):
         lat.set_engine(engine_id(imex, engine))
     except imex.ImexError:
         lat.close()
-        pytest.skip(f"{engine} engine not available in this build")
+        pytest.skip(f"{engine} engine not available")
     return lat
 
 
