@@ -173,6 +173,7 @@ constexpr int kThreads = 128;
 // its row; with P a multiple of 4 the interior of every row starts on a
 // 32-byte sector, so a warp's 32 values are 8 whole sectors.
 constexpr int kZOff = 3;
+static_assert(kZOff == 3, "push_halo stores the low z ghost as the last word of its row's first 32-byte sector");
 struct PadGeom {
     int L[3];
     int P;
@@ -231,6 +232,26 @@ __device__ __forceinline__ void push_halo(const BlockDev* __restrict__ blocks, i
         t[axis] = side == 1 ? 0 : ng.L[axis] + 1;
         const size_t base = pad_index(ng, t[0], t[1], t[2]);
         T* dst = reinterpret_cast<T*>(N.buf[buf]);
+        // A z-face ghost value is alone in its row's first (last) 32-byte
+        // sector with pad words nothing reads; a single 8-byte store leaves
+        // the sector partly written and costs a read-modify-write when it
+        // leaves L2, so the whole sector is stored: the value and zeroed
+        // pads, as two 16-byte stores.  The low ghost (padded z 0, word
+        // kZOff of the row) always ends its row's first sector; the high one (word Lz + kZOff + 1) starts a sector when Lz is a
+        // multiple of 4, the pitch then leaving three pad words after it.
+        if (axis == 2 && (side == 1 || (ng.L[2] & 3) == 0)) {
+            const size_t s0 = side == 1 ? base - kZOff : base;  // the sector's first word
+#pragma unroll
+            for (int a = 0; a < kQ; ++a)
+                if (ex(a, 2) == side) {
+                    unsigned long long w;
+                    memcpy(&w, &v[a], sizeof w);
+                    auto* q = reinterpret_cast<ulonglong2*>(dst + (size_t)a * ng.plane + s0);
+                    q[0] = side == 1 ? make_ulonglong2(0ull, 0ull) : make_ulonglong2(w, 0ull);
+                    q[1] = side == 1 ? make_ulonglong2(0ull, w) : make_ulonglong2(0ull, 0ull);
+                }
+            return;
+        }
 #pragma unroll
         for (int a = 0; a < kQ; ++a) {
             const int e = axis == 0 ? ex(a, 0) : axis == 1 ? ex(a, 1) : ex(a, 2);
