@@ -250,29 +250,46 @@ __device__ __forceinline__ void run_items(const ItemOf& item_of, int my, int sta
     if (issuer)
         for (int t = 0; t < stages - 1 && t < my; ++t) issue(t);
 
+    // A copy did not complete: record it, wait (bounded) for the copies
+    // this CTA still has in flight (items t .. t + stages - 1), and stop.
+    auto fail_at = [&](int t) {
+        if (threadIdx.x == 0) {
+            atomicOr(wc.err, 1u);
+            const int last = t + stages - 1 < my ? t + stages - 1 : my - 1;
+            for (int q = t; q <= last; ++q)
+                bulk::mbar_wait(&full[q % stages], (uint32_t)((q / stages) & 1), wc.cycles);
+        }
+        __syncthreads();
+    };
     for (int t = 0; t < my; ++t) {
         const int s = t % stages;
         if (issuer && t + stages - 1 < my) issue(t + stages - 1);
         const int ok = bulk::mbar_wait(&full[s], (uint32_t)((t / stages) & 1), wc.cycles);
-        if (__syncthreads_or(!ok)) {
-            // A copy did not complete: record it, wait (bounded) for the
-            // copies this CTA still has in flight, and stop.
-            if (threadIdx.x == 0) {
-                atomicOr(wc.err, 1u);
-                const int last = t + stages - 1 < my ? t + stages - 1 : my - 1;
-                for (int q = t; q <= last; ++q)
-                    bulk::mbar_wait(&full[q % stages], (uint32_t)((q / stages) & 1), wc.cycles);
-            }
-            __syncthreads();
+        // One lattice: every thread starts on the item together (measured
+        // faster: 59.0 against 55.7 GLUPS at 256^3 float16).  A batch: each
+        // warp starts once it sees the stage full, a thread whose wait ran
+        // out skips the item, and the barrier that ends the item tells every
+        // thread (62.3 against 58.5 GLUPS on four 256^3 float16 lattices).
+        if (!kSlots && __syncthreads_or(!ok)) {
+            fail_at(t);
             return;
         }
         const Item& it = kSlots ? slots[t % nslots] : item_of(t);
-        if (it.active) {
+        if (ok && it.active) {
             if (it.prec == IMEX_F32) compute_item<IMEX_F32, kDirBytes, Ar>(ring + (size_t)s * kStage, it, base);
             else compute_item<IMEX_F16DEV, kDirBytes, Ar>(ring + (size_t)s * kStage, it, base);
         }
-        if (threadIdx.x == 0 && t + stages < my) arm(t + stages);  // stage s, next use
-        __syncthreads();  // stage s may be refilled
+        // stage s, next use: armed only on a phase thread 0 saw complete
+        // (an arrival on a phase still pending would be one too many)
+        if (threadIdx.x == 0 && ok && t + stages < my) arm(t + stages);
+        if (kSlots) {
+            if (__syncthreads_or(!ok)) {  // stage s may be refilled - unless a copy did not complete
+                fail_at(t);
+                return;
+            }
+        } else {
+            __syncthreads();  // stage s may be refilled
+        }
     }
 }
 
