@@ -211,11 +211,20 @@ __device__ __forceinline__ void run_items(const ItemOf& item_of, int my, int sta
     const bool issuer = my_dir < kQ;
 
     const int nslots = stages + 1;
-    auto arm = [&](int t) {  // thread 0
+    // Thread 0 describes item t and arms its stage's next phase.  An item
+    // with no bytes (a batch member done for the tick) completes that phase
+    // at its arrival; with defer_empty the arrival is left to the caller
+    // (returns true), who makes it only once every thread has passed its
+    // wait on the stage's previous phase - completed early, the phase would
+    // flip the stage's parity back under a thread still waiting on it, and
+    // that thread's parity wait would run out.
+    auto arm = [&](int t, bool defer_empty) -> bool {
         const Item it = item_of(t);
         if (kSlots) slots[t % nslots] = it;
+        if (!it.active && defer_empty) return true;
         const uint32_t bytes = it.active ? (uint32_t)kQ * it.B * it.nz * elem_bytes(it.prec) : 0u;
         bulk::mbar_arrive_expect_tx(&full[t % stages], bytes);
+        return false;
     };
     auto issue = [&](int t) {  // after the barrier that follows arm(t)
         const Item it = kSlots ? slots[t % nslots] : item_of(t);
@@ -244,7 +253,7 @@ __device__ __forceinline__ void run_items(const ItemOf& item_of, int my, int sta
     if (threadIdx.x == 0) {
         for (int q = 0; q < stages; ++q) bulk::mbar_init(&full[q], 1);
         bulk::fence_mbar_init();
-        for (int t = 0; t < stages && t < my; ++t) arm(t);  // first item of every stage
+        for (int t = 0; t < stages && t < my; ++t) arm(t, false);  // first item of every stage (no waits yet)
     }
     __syncthreads();
     if (issuer)
@@ -280,13 +289,17 @@ __device__ __forceinline__ void run_items(const ItemOf& item_of, int my, int sta
             else compute_item<IMEX_F16DEV, kDirBytes, Ar>(ring + (size_t)s * kStage, it, base);
         }
         // stage s, next use: armed only on a phase thread 0 saw complete
-        // (an arrival on a phase still pending would be one too many)
-        if (threadIdx.x == 0 && ok && t + stages < my) arm(t + stages);
+        // (an arrival on a phase still pending would be one too many); in a
+        // batch other warps may still be waiting on stage s, so an item with
+        // no bytes arrives after the barrier
+        bool owed = false;
+        if (threadIdx.x == 0 && ok && t + stages < my) owed = arm(t + stages, kSlots);
         if (kSlots) {
             if (__syncthreads_or(!ok)) {  // stage s may be refilled - unless a copy did not complete
                 fail_at(t);
                 return;
             }
+            if (owed) bulk::mbar_arrive_expect_tx(&full[s], 0u);
         } else {
             __syncthreads();  // stage s may be refilled
         }

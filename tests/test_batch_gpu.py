@@ -259,3 +259,29 @@ def test_segment_kernel_graph_after_a_retune_moves_its_group_table(imex):
             assert np.array_equal(lat.get_f(), alone(imex, s, lat.steps_done()))
     for lat in lats:
         lat.close()
+
+
+@pytest.mark.parametrize("row_shape", [(2, 4, 1), (2, 2, 2), (3, 1, 2)])
+def test_row_kernel_many_members_stopping_mid_tick(imex, row_shape):
+    """Many float16 members reaching their step limits at staggered steps
+    inside the row kernel's ticks: every tick mixes items with bytes and
+    items without (a stopped member's), which complete their stage's phase
+    on arrival.  Every member ends where it ends alone, at its limit."""
+    rng = np.random.default_rng(5)
+    specs, limits = [], []
+    for q in range(12):
+        edge = int(rng.choice([16, 24, 32]))
+        specs.append(((edge, edge, edge), "f16dev", 0.01, 0.05, (0.1 * q, 0.2 * q, 0.3 * q)))
+        limits.append(int(rng.integers(1, 60)))
+    lats = [make(imex, s) for s in specs]
+    with imex.Batch(16) as b:
+        b.set_row_launch(*row_shape)
+        b.set_graph(25)
+        for lat, lim in zip(lats, limits):
+            b.add(lat, lim)
+        b.step(75)
+        b.synchronize()
+    for lat, spec, lim in zip(lats, specs, limits):
+        assert lat.steps_done() == lim
+        assert np.array_equal(lat.get_f(), alone(imex, spec, lim))
+        lat.close()
